@@ -1,0 +1,169 @@
+"""ORACLE loader — test infrastructure, not product code.
+
+Compiles and loads the plain-C restatement of the reference algorithm
+(oracle/par2_oracle.c) and, where it has been built, the reference's own CPU
+implementation (oracle/_ref/libparref.so, see oracle/ref.mk).  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "par2_oracle.c")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD_DIR, "libpar2oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libparref.so")
+
+_lib = None
+_ref = None
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with gcc (portable C, no ISA-specific flags)."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        os.makedirs(BUILD_DIR, exist_ok=True)
+        tmp = LIB + ".tmp.%d" % os.getpid()
+        subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-pthread", "-std=gnu99",
+                               "-fno-strict-aliasing", "-o", tmp, SRC])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(build())
+        u16, sz, vp, i32 = ctypes.c_uint16, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int
+        L.or_exp.restype = u16; L.or_exp.argtypes = [ctypes.c_uint32]
+        L.or_mul.restype = u16; L.or_mul.argtypes = [u16, u16]
+        L.or_mul_slow.restype = u16; L.or_mul_slow.argtypes = [u16, u16]
+        L.or_input_log.restype = u16; L.or_input_log.argtypes = [u16]
+        L.or_coeff.restype = u16; L.or_coeff.argtypes = [u16, u16]
+        L.or_coeff_from_log.restype = u16; L.or_coeff_from_log.argtypes = [u16, u16]
+        L.or_recover.restype = i32
+        L.or_recover.argtypes = [vp, vp, vp, ctypes.c_uint, sz, vp, ctypes.c_uint, vp, i32]
+        L.or_recover_coeffs.restype = i32
+        L.or_recover_coeffs.argtypes = [vp, vp, vp, ctypes.c_uint, sz, ctypes.c_uint, vp, i32]
+        L.or_cksum.restype = ctypes.c_uint64; L.or_cksum.argtypes = [vp, sz, sz]
+        L.or_cksum_check.restype = i32; L.or_cksum_check.argtypes = [vp, sz, ctypes.c_uint64]
+        L.or_md5.restype = None; L.or_md5.argtypes = [vp, sz, ctypes.c_uint64, vp]
+        L.or_crc32.restype = ctypes.c_uint32; L.or_crc32.argtypes = [vp, sz, ctypes.c_uint64]
+        L.or_hash_file.restype = None; L.or_hash_file.argtypes = [vp, sz, sz, vp, vp]
+        L.or_hash_rows.restype = None
+        L.or_hash_rows.argtypes = [vp, sz, sz, vp, ctypes.c_uint, vp, vp, i32]
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def ref():
+    """The reference's own compiled CPU core (only where oracle/ref.mk ran)."""
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise FileNotFoundError(REF_LIB)
+        L = ctypes.CDLL(REF_LIB)
+        u16, sz, vp, i32 = ctypes.c_uint16, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int
+        L.ref_gf_exp.restype = u16; L.ref_gf_exp.argtypes = [u16]
+        L.ref_input_log.restype = u16; L.ref_input_log.argtypes = [u16]
+        L.ref_coeff.restype = u16; L.ref_coeff.argtypes = [u16, u16]
+        L.ref_cksum_copy.restype = None; L.ref_cksum_copy.argtypes = [vp, vp, sz, sz]
+        L.ref_cksum_copy_check.restype = i32; L.ref_cksum_copy_check.argtypes = [vp, vp, sz]
+        L.ref_create.restype = i32
+        L.ref_create.argtypes = [vp, vp, vp, ctypes.c_uint, sz, vp, ctypes.c_uint, vp, vp, i32, i32,
+                                 ctypes.c_uint, ctypes.POINTER(ctypes.c_double)]
+        L.ref_create_coeffs.restype = i32
+        L.ref_create_coeffs.argtypes = [vp, vp, vp, ctypes.c_uint, sz, ctypes.c_uint, vp, vp, i32]
+        L.ref_last_method_name.restype = ctypes.c_char_p
+        L.ref_hash_file.restype = None; L.ref_hash_file.argtypes = [vp, sz, sz, sz, vp, vp]
+        L.ref_crc32.restype = ctypes.c_uint32; L.ref_crc32.argtypes = [vp, sz]
+        L.ref_md5crc.restype = ctypes.c_uint32; L.ref_md5crc.argtypes = [vp, sz, sz, vp]
+        L.ref_md5multi.restype = None; L.ref_md5multi.argtypes = [vp, ctypes.c_uint, sz, vp]
+        _ref = L
+    return _ref
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+# ---------------------------------------------------------------- helpers
+def recover(inputs: np.ndarray, lens, input_nums, exps, threads: int = 1) -> np.ndarray:
+    """inputs: uint8 [n, slice]; returns uint8 [r, slice] recovery slices."""
+    inputs = np.ascontiguousarray(inputs, dtype=np.uint8)
+    n, S = inputs.shape
+    lens = np.ascontiguousarray(lens, dtype=np.uint64)
+    nums = np.ascontiguousarray(input_nums, dtype=np.uint16)
+    exps = np.ascontiguousarray(exps, dtype=np.uint16)
+    out = np.zeros((len(exps), S), dtype=np.uint8)
+    rc = lib().or_recover(_p(inputs), _p(lens), _p(nums), n, S, _p(exps), len(exps), _p(out), threads)
+    if rc:
+        raise RuntimeError("oracle recover failed: %d" % rc)
+    return out
+
+
+def recover_coeffs(inputs: np.ndarray, lens, coeffs_rn: np.ndarray, threads: int = 1) -> np.ndarray:
+    inputs = np.ascontiguousarray(inputs, dtype=np.uint8)
+    n, S = inputs.shape
+    lens = np.ascontiguousarray(lens, dtype=np.uint64)
+    c = np.ascontiguousarray(coeffs_rn, dtype=np.uint16)
+    r = c.shape[0]
+    out = np.zeros((r, S), dtype=np.uint8)
+    rc = lib().or_recover_coeffs(_p(inputs), _p(lens), _p(c), n, S, r, _p(out), threads)
+    if rc:
+        raise RuntimeError("oracle recover failed: %d" % rc)
+    return out
+
+
+def coeff(i: int, e: int) -> int:
+    return lib().or_coeff(i, e)
+
+
+def cksum(data: bytes | np.ndarray, slice_len: int | None = None) -> int:
+    a = np.frombuffer(bytes(data), dtype=np.uint8) if not isinstance(data, np.ndarray) else np.ascontiguousarray(data, dtype=np.uint8)
+    if slice_len is None:
+        slice_len = a.size
+    return lib().or_cksum(_p(a), a.size, slice_len)
+
+
+def md5(data, zero_pad: int = 0) -> bytes:
+    a = np.frombuffer(bytes(data), dtype=np.uint8) if not isinstance(data, np.ndarray) else np.ascontiguousarray(data, dtype=np.uint8)
+    out = np.zeros(16, dtype=np.uint8)
+    lib().or_md5(_p(a), a.size, zero_pad, _p(out))
+    return out.tobytes()
+
+
+def crc32(data, zero_pad: int = 0) -> int:
+    a = np.frombuffer(bytes(data), dtype=np.uint8) if not isinstance(data, np.ndarray) else np.ascontiguousarray(data, dtype=np.uint8)
+    return lib().or_crc32(_p(a), a.size, zero_pad)
+
+
+def hash_file(data: np.ndarray, slice_size: int):
+    a = np.ascontiguousarray(data, dtype=np.uint8)
+    ns = (a.size + slice_size - 1) // slice_size
+    ifsc = np.zeros(max(ns, 1) * 20, dtype=np.uint8)
+    fmd5 = np.zeros(16, dtype=np.uint8)
+    lib().or_hash_file(_p(a), a.size, slice_size, _p(ifsc), _p(fmd5))
+    return ifsc[: ns * 20].tobytes(), fmd5.tobytes()
+
+
+def hash_rows(rows: np.ndarray, lens=None, threads: int = 1):
+    """MD5 + CRC32 of each row of a uint8 [n, S] array (row i zero-padded from lens[i])."""
+    rows = np.ascontiguousarray(rows, dtype=np.uint8)
+    n, S = rows.shape
+    md5s = np.zeros((n, 16), dtype=np.uint8)
+    crcs = np.zeros(n, dtype=np.uint32)
+    lp = None
+    if lens is not None:
+        lens = np.ascontiguousarray(lens, dtype=np.uint64)
+        lp = _p(lens)
+    lib().or_hash_rows(_p(rows), S, S, lp, n, _p(md5s), _p(crcs), threads)
+    return md5s, crcs

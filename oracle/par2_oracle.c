@@ -1,0 +1,379 @@
+/*
+ * ORACLE — test infrastructure, not product code.
+ *
+ * A plain-C restatement of the reference's CPU algorithm for the PAR2 recovery
+ * path (ParPar, Ravencentric/ParPar).  It is the checker for the CUDA path:
+ * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+ * it.  The product library (libpar2cuda.so) never links or calls it.
+ *
+ * Parity pin: every function below is checked against the reference's own
+ * compiled code (oracle/ref.mk -> oracle/_ref/libparref.so, driven by
+ * oracle/ref_shim.cpp) through the golden fixtures in tests/golden/, which
+ * tests/golden/make_golden.py generates from that build.
+ *
+ * Contents (reference file:line each function follows):
+ *   GF(2^16), polynomial 0x1100B ............ gf16/gf16_global.h:9-10
+ *   PAR2 input logs / coefficients .......... gf16/gfmat_coeff.c:6-77
+ *   region multiply-accumulate (LOOKUP) ..... gf16/gf16_lookup.c:124-181, 218-249
+ *   recovery computation .................... gf16/controller_cpu.cpp:372-385, 463-537
+ *   exponent-0 row = XOR of inputs .......... gf16/controller_cpu.cpp:498-512
+ *   internal checksum (generic, 8-byte) ..... gf16/gf16_checksum_generic.h:25-130,
+ *                                             gf16/gf16_cksum_base.h:13-60
+ *   MD5 (RFC 1321) + zero-pad finish ........ hasher/md5-final.c:4-60
+ *   CRC32 (reflected 0xEDB88320) + zero pad . hasher/crc_zeropad.c:7-66
+ *   IFSC entries / file MD5 ................. hasher/hasher_base.h:103-186
+ */
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define OR_POLY 0x1100Bu
+
+static uint16_t or_exp_tab[65536 * 2];
+static uint16_t or_log_tab[65536];
+static uint16_t or_in_log[32768];
+static int or_ready = 0;
+static pthread_once_t or_once = PTHREAD_ONCE_INIT;
+
+static void or_build(void) {
+	uint32_t n = 1;
+	for(uint32_t e = 0; e < 65535; e++) {
+		or_exp_tab[e] = (uint16_t)n;
+		or_exp_tab[e + 65535] = (uint16_t)n;
+		or_log_tab[n] = (uint16_t)e;
+		n <<= 1;
+		if(n & 0x10000) n ^= OR_POLY;
+	}
+	or_exp_tab[131070] = or_exp_tab[0];
+	or_exp_tab[131071] = or_exp_tab[1];
+	or_log_tab[0] = 0;
+	/* gfmat_coeff.c:12-22 — input i gets the i-th exponent (counting from 1)
+	 * that is not divisible by 3, 5, 17 or 257, i.e. coprime with 65535 */
+	uint32_t e = 0;
+	for(uint32_t i = 0; i < 32768; i++) {
+		do { e++; } while(e % 3 == 0 || e % 5 == 0 || e % 17 == 0 || e % 257 == 0);
+		or_in_log[i] = (uint16_t)e;
+	}
+	or_ready = 1;
+}
+
+void or_init(void) { pthread_once(&or_once, or_build); }
+
+/* 2^v for any v (reduced mod 65535) — gf16_exp, gfmat_coeff.c:43-54 */
+uint16_t or_exp(uint32_t v) { or_init(); return or_exp_tab[v % 65535u]; }
+
+uint16_t or_mul(uint16_t a, uint16_t b) {
+	or_init();
+	if(!a || !b) return 0;
+	return or_exp_tab[(uint32_t)or_log_tab[a] + or_log_tab[b]];
+}
+
+/* shift-and-xor multiply, independent of the tables (cross-check) */
+uint16_t or_mul_slow(uint16_t a, uint16_t b) {
+	uint32_t p = 0, x = a;
+	for(int i = 0; i < 16; i++) {
+		if(b >> i & 1) p ^= x;
+		x <<= 1;
+		if(x & 0x10000) x ^= OR_POLY;
+	}
+	return (uint16_t)p;
+}
+
+uint16_t or_input_log(uint16_t input) { or_init(); return or_in_log[input & 32767]; }
+
+/* gfmat_coeff.c:60-77: coefficient = 2^((log_i * e) mod 65535) */
+uint16_t or_coeff_from_log(uint16_t inLog, uint16_t exponent) {
+	or_init();
+	return or_exp_tab[((uint32_t)inLog * exponent) % 65535u];
+}
+uint16_t or_coeff(uint16_t input, uint16_t exponent) {
+	return or_coeff_from_log(or_input_log(input), exponent);
+}
+
+/* Split 8-bit tables for multiply by c: c*x = lo[x & 255] ^ hi[x >> 8]
+ * (the LOOKUP method's two 256-entry tables, gf16_lookup.c:124-181). */
+static void or_tables(uint16_t c, uint16_t* lo, uint16_t* hi) {
+	for(unsigned v = 0; v < 256; v++) {
+		lo[v] = or_mul(c, (uint16_t)v);
+		hi[v] = or_mul(c, (uint16_t)(v << 8));
+	}
+}
+
+/* dst[w] ^= c * src[w] over `words` little-endian u16 words */
+void or_muladd_region(uint8_t* dst, const uint8_t* src, size_t words, uint16_t c) {
+	uint16_t lo[256], hi[256];
+	or_init();
+	or_tables(c, lo, hi);
+	for(size_t w = 0; w < words; w++) {
+		uint16_t x = (uint16_t)(src[2 * w] | (src[2 * w + 1] << 8));
+		uint16_t y = (uint16_t)(dst[2 * w] | (dst[2 * w + 1] << 8));
+		y ^= lo[x & 255] ^ hi[x >> 8];
+		dst[2 * w] = (uint8_t)y;
+		dst[2 * w + 1] = (uint8_t)(y >> 8);
+	}
+}
+
+/* ---------- recovery computation (multi-threaded LOOKUP port) ---------- */
+typedef struct {
+	const uint8_t* inputs; const size_t* lens; const uint16_t* coeffs; /* [r][n] */
+	unsigned n, r; size_t slice; uint8_t* out;
+	size_t chunk; unsigned nchunks; unsigned nthreads; unsigned tid;
+} or_job;
+
+static void* or_worker(void* arg) {
+	or_job* j = (or_job*)arg;
+	uint16_t* lo = (uint16_t*)malloc(256 * sizeof(uint16_t) * 2);
+	uint16_t* hi = lo + 256;
+	/* static split of (byte chunk × recovery row) units, as run_kernel does
+	 * (controller_cpu.cpp:539-624) */
+	size_t units = (size_t)j->nchunks * j->r;
+	for(size_t u = j->tid; u < units; u += j->nthreads) {
+		unsigned ch = (unsigned)(u / j->r), row = (unsigned)(u % j->r);
+		size_t off = (size_t)ch * j->chunk;
+		size_t len = j->slice - off < j->chunk ? j->slice - off : j->chunk;
+		uint8_t* dst = j->out + (size_t)row * j->slice + off;
+		memset(dst, 0, len);
+		for(unsigned i = 0; i < j->n; i++) {
+			uint16_t c = j->coeffs[(size_t)row * j->n + i];
+			size_t have = j->lens[i] > off ? j->lens[i] - off : 0; /* zero padding beyond lens[i] */
+			if(have > len) have = len;
+			if(!have || !c) continue;
+			const uint8_t* src = j->inputs + (size_t)i * j->slice + off;
+			or_tables(c, lo, hi);
+			size_t w = 0;
+			for(; 2 * w + 1 < have; w++) {
+				uint16_t x = (uint16_t)(src[2 * w] | (src[2 * w + 1] << 8));
+				uint16_t p = lo[x & 255] ^ hi[x >> 8];
+				dst[2 * w] ^= (uint8_t)p;
+				dst[2 * w + 1] ^= (uint8_t)(p >> 8);
+			}
+			if(2 * w < have) { /* odd tail byte: high byte is zero padding */
+				uint16_t p = lo[src[2 * w]];
+				dst[2 * w] ^= (uint8_t)p;
+				dst[2 * w + 1] ^= (uint8_t)(p >> 8);
+			}
+		}
+	}
+	free(lo);
+	return NULL;
+}
+
+/* inputs: n rows of `slice` bytes (row i meaningful up to lens[i], zero beyond);
+ * coeffs: [r][n]; out: r rows of `slice` bytes.  slice must be even. */
+int or_recover_coeffs(const uint8_t* inputs, const size_t* lens, const uint16_t* coeffs,
+                      unsigned n, size_t slice, unsigned r, uint8_t* out, int threads) {
+	or_init();
+	if(slice & 1) return -1;
+	if(threads < 1) threads = 1;
+	if(threads > 256) threads = 256;
+	size_t chunk = 32768;
+	if(chunk > slice) chunk = slice;
+	unsigned nchunks = (unsigned)((slice + chunk - 1) / chunk);
+	pthread_t th[256];
+	or_job jobs[256];
+	for(int t = 0; t < threads; t++) {
+		or_job jb = {inputs, lens, coeffs, n, r, slice, out, chunk, nchunks, (unsigned)threads, (unsigned)t};
+		jobs[t] = jb;
+	}
+	if(threads == 1) { or_worker(&jobs[0]); return 0; }
+	for(int t = 0; t < threads; t++) pthread_create(&th[t], NULL, or_worker, &jobs[t]);
+	for(int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+	return 0;
+}
+
+/* PAR2 recovery: coefficients from input numbers and recovery exponents
+ * (set_coeffs, controller_cpu.cpp:372-379) */
+int or_recover(const uint8_t* inputs, const size_t* lens, const uint16_t* inputNums, unsigned n,
+               size_t slice, const uint16_t* exps, unsigned r, uint8_t* out, int threads) {
+	or_init();
+	uint16_t* coeffs = (uint16_t*)malloc(sizeof(uint16_t) * (size_t)n * r + 2);
+	if(!coeffs) return -2;
+	for(unsigned row = 0; row < r; row++)
+		for(unsigned i = 0; i < n; i++)
+			coeffs[(size_t)row * n + i] = or_coeff(inputNums[i], exps[row]);
+	int rc = or_recover_coeffs(inputs, lens, coeffs, n, slice, r, out, threads);
+	free(coeffs);
+	return rc;
+}
+
+/* ---------- internal GF checksum, generic 8-byte block (4 u16 lanes) ---------- */
+static inline uint64_t or_mul2x4(uint64_t v) {
+	const uint64_t m = 0x0001000100010001ULL;
+	return ((v << 1) & ~m) ^ (((v >> 15) & m) * (OR_POLY & 0xFFFF));
+}
+static inline uint64_t or_rd64(const uint8_t* p, size_t avail) {
+	uint64_t v = 0;
+	for(size_t b = 0; b < 8 && b < avail; b++) v |= (uint64_t)p[b] << (8 * b);
+	return v;
+}
+/* multiply each lane by 2^e (gf16_checksum_exp_generic) */
+static uint64_t or_ck_exp(uint64_t ck, uint32_t e) {
+	uint16_t c = or_exp(e);
+	uint64_t res = 0;
+	for(int b = 15; b >= 0; b--) {
+		res = or_mul2x4(res);
+		if(c >> b & 1) res ^= ck;
+	}
+	return res;
+}
+/* Checksum of `srcLen` bytes zero-padded to `sliceLen` (gf16_cksum_copy):
+ * Horner over 8-byte blocks, ck = mul2(ck) ^ block, then the zero tail
+ * multiplies by 2^(tail blocks). */
+uint64_t or_cksum(const uint8_t* src, size_t srcLen, size_t sliceLen) {
+	or_init();
+	uint64_t ck = 0;
+	for(size_t p = 0; p < srcLen; p += 8) ck = or_mul2x4(ck) ^ or_rd64(src + p, srcLen - p);
+	size_t done = (srcLen + 7) / 8 * 8;
+	if(srcLen < sliceLen && done < sliceLen)
+		ck = or_ck_exp(ck, (uint32_t)(((sliceLen - done + 7) / 8) % 65535));
+	return ck;
+}
+/* Verifies `len` bytes against their carried checksum (gf16_cksum_copy_check):
+ * rewind by 2^-(blocks), re-run Horner over the data, require zero. */
+int or_cksum_check(const uint8_t* data, size_t len, uint64_t ck) {
+	or_init();
+	uint32_t nb = (uint32_t)(((len + 7) / 8) % 65535);
+	ck = or_ck_exp(ck, 65535 - nb);
+	for(size_t p = 0; p < len; p += 8) ck = or_mul2x4(ck) ^ or_rd64(data + p, len - p);
+	return ck == 0;
+}
+
+/* ---------- MD5 (RFC 1321) ---------- */
+static const uint32_t or_md5_k[64] = {
+	0xd76aa478,0xe8c7b756,0x242070db,0xc1bdceee,0xf57c0faf,0x4787c62a,0xa8304613,0xfd469501,
+	0x698098d8,0x8b44f7af,0xffff5bb1,0x895cd7be,0x6b901122,0xfd987193,0xa679438e,0x49b40821,
+	0xf61e2562,0xc040b340,0x265e5a51,0xe9b6c7aa,0xd62f105d,0x02441453,0xd8a1e681,0xe7d3fbc8,
+	0x21e1cde6,0xc33707d6,0xf4d50d87,0x455a14ed,0xa9e3e905,0xfcefa3f8,0x676f02d9,0x8d2a4c8a,
+	0xfffa3942,0x8771f681,0x6d9d6122,0xfde5380c,0xa4beea44,0x4bdecfa9,0xf6bb4b60,0xbebfbc70,
+	0x289b7ec6,0xeaa127fa,0xd4ef3085,0x04881d05,0xd9d4d039,0xe6db99e5,0x1fa27cf8,0xc4ac5665,
+	0xf4292244,0x432aff97,0xab9423a7,0xfc93a039,0x655b59c3,0x8f0ccc92,0xffeff47d,0x85845dd1,
+	0x6fa87e4f,0xfe2ce6e0,0xa3014314,0x4e0811a1,0xf7537e82,0xbd3af235,0x2ad7d2bb,0xeb86d391};
+static const uint8_t or_md5_r[64] = {7,12,17,22,7,12,17,22,7,12,17,22,7,12,17,22,5,9,14,20,5,9,14,20,5,9,14,20,5,9,14,20,
+	4,11,16,23,4,11,16,23,4,11,16,23,4,11,16,23,6,10,15,21,6,10,15,21,6,10,15,21,6,10,15,21};
+
+static void or_md5_block(uint32_t* st, const uint8_t* blk) {
+	uint32_t m[16];
+	for(int i = 0; i < 16; i++)
+		m[i] = (uint32_t)blk[4*i] | ((uint32_t)blk[4*i+1] << 8) | ((uint32_t)blk[4*i+2] << 16) | ((uint32_t)blk[4*i+3] << 24);
+	uint32_t a = st[0], b = st[1], c = st[2], d = st[3];
+	for(int i = 0; i < 64; i++) {
+		uint32_t f; int g;
+		if(i < 16) { f = (b & c) | (~b & d); g = i; }
+		else if(i < 32) { f = (d & b) | (~d & c); g = (5 * i + 1) & 15; }
+		else if(i < 48) { f = b ^ c ^ d; g = (3 * i + 5) & 15; }
+		else { f = c ^ (b | ~d); g = (7 * i) & 15; }
+		uint32_t t = a + f + or_md5_k[i] + m[g];
+		a = d; d = c; c = b;
+		b = b + ((t << or_md5_r[i]) | (t >> (32 - or_md5_r[i])));
+	}
+	st[0] += a; st[1] += b; st[2] += c; st[3] += d;
+}
+
+/* MD5 of data[0..len) followed by zeroPad zero bytes (md5_final_block semantics) */
+void or_md5(const uint8_t* data, size_t len, uint64_t zeroPad, uint8_t out[16]) {
+	uint32_t st[4] = {0x67452301, 0xefcdab89, 0x98badcfe, 0x10325476};
+	uint8_t blk[64];
+	uint64_t total = len + zeroPad;
+	size_t p = 0;
+	for(; p + 64 <= len; p += 64) or_md5_block(st, data + p);
+	size_t rem = len - p;
+	memcpy(blk, data + p, rem);
+	uint64_t pad = zeroPad;
+	while(rem + pad >= 64) { /* zero-filled blocks */
+		memset(blk + rem, 0, 64 - rem);
+		or_md5_block(st, blk);
+		pad -= 64 - rem;
+		rem = 0;
+	}
+	memset(blk + rem, 0, 64 - rem);
+	rem += (size_t)pad;
+	blk[rem++] = 0x80;
+	if(rem > 56) { memset(blk + rem, 0, 64 - rem); or_md5_block(st, blk); rem = 0; memset(blk, 0, 64); }
+	memset(blk + rem, 0, 56 - rem);
+	uint64_t bits = total << 3;
+	for(int i = 0; i < 8; i++) blk[56 + i] = (uint8_t)(bits >> (8 * i));
+	or_md5_block(st, blk);
+	for(int i = 0; i < 4; i++) {
+		out[4*i] = (uint8_t)st[i]; out[4*i+1] = (uint8_t)(st[i] >> 8);
+		out[4*i+2] = (uint8_t)(st[i] >> 16); out[4*i+3] = (uint8_t)(st[i] >> 24);
+	}
+}
+
+/* ---------- CRC32 (IEEE, reflected) ---------- */
+static uint32_t or_crc_tab[256];
+static pthread_once_t or_crc_once = PTHREAD_ONCE_INIT;
+static void or_crc_build(void) {
+	for(uint32_t i = 0; i < 256; i++) {
+		uint32_t c = i;
+		for(int k = 0; k < 8; k++) c = (c >> 1) ^ (0xEDB88320u & (0u - (c & 1)));
+		or_crc_tab[i] = c;
+	}
+}
+/* a*b mod P in the reflected bit order (bit 31 = x^0) */
+static uint32_t or_crc_mulmod(uint32_t a, uint32_t b) {
+	uint32_t r = 0;
+	for(int i = 0; i < 32; i++) {
+		if(b & 0x80000000u) r ^= a;
+		b <<= 1;
+		a = (a >> 1) ^ (0xEDB88320u & (0u - (a & 1)));
+	}
+	return r;
+}
+/* CRC of data followed by zeroPad zero bytes (crc_zeroPad: multiply the raw
+ * state by x^(8*zeroPad) by square-and-multiply) */
+uint32_t or_crc32(const uint8_t* data, size_t len, uint64_t zeroPad) {
+	pthread_once(&or_crc_once, or_crc_build);
+	uint32_t c = 0xFFFFFFFFu;
+	for(size_t i = 0; i < len; i++) c = (c >> 8) ^ or_crc_tab[(c ^ data[i]) & 255];
+	uint32_t xn = 0x00800000u; /* x^8 in reflected order */
+	while(zeroPad) {
+		if(zeroPad & 1) c = or_crc_mulmod(c, xn);
+		xn = or_crc_mulmod(xn, xn);
+		zeroPad >>= 1;
+	}
+	return ~c;
+}
+
+/* IFSC entries of one file (20 bytes per slice: MD5 then CRC32 little-endian,
+ * last slice zero-padded to sliceSize) and the file MD5 (no padding). */
+void or_hash_file(const uint8_t* data, size_t len, size_t sliceSize, uint8_t* ifsc, uint8_t fileMd5[16]) {
+	size_t nslices = (len + sliceSize - 1) / sliceSize;
+	for(size_t s = 0; s < nslices; s++) {
+		size_t off = s * sliceSize;
+		size_t n = len - off < sliceSize ? len - off : sliceSize;
+		or_md5(data + off, n, sliceSize - n, ifsc + 20 * s);
+		uint32_t crc = or_crc32(data + off, n, sliceSize - n);
+		for(int b = 0; b < 4; b++) ifsc[20 * s + 16 + b] = (uint8_t)(crc >> (8 * b));
+	}
+	or_md5(data, len, 0, fileMd5);
+}
+
+/* ---------- MD5 of many equal-length buffers (threaded; hashing baseline) ---------- */
+typedef struct { const uint8_t* base; size_t stride, len; const size_t* lens; uint64_t pad; unsigned n, nt, tid; uint8_t* md5; uint32_t* crc; } or_hjob;
+static void* or_hworker(void* arg) {
+	or_hjob* j = (or_hjob*)arg;
+	for(unsigned i = j->tid; i < j->n; i += j->nt) {
+		size_t l = j->lens ? j->lens[i] : j->len;
+		uint64_t pad = j->lens ? (uint64_t)(j->len - l) : j->pad;
+		or_md5(j->base + (size_t)i * j->stride, l, pad, j->md5 + 16 * (size_t)i);
+		if(j->crc) j->crc[i] = or_crc32(j->base + (size_t)i * j->stride, l, pad);
+	}
+	return NULL;
+}
+/* MD5 (+ optional CRC32) of n rows; row i holds lens[i] bytes zero-padded to len
+ * (lens may be NULL: every row is `len` bytes). */
+void or_hash_rows(const uint8_t* base, size_t stride, size_t len, const size_t* lens, unsigned n,
+                  uint8_t* md5, uint32_t* crc, int threads) {
+	pthread_once(&or_crc_once, or_crc_build);
+	if(threads < 1) threads = 1;
+	if(threads > 256) threads = 256;
+	pthread_t th[256];
+	or_hjob jobs[256];
+	for(int t = 0; t < threads; t++) {
+		or_hjob jb = {base, stride, len, lens, 0, n, (unsigned)threads, (unsigned)t, md5, crc};
+		jobs[t] = jb;
+	}
+	for(int t = 0; t < threads; t++) pthread_create(&th[t], NULL, or_hworker, &jobs[t]);
+	for(int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+}
