@@ -1,0 +1,179 @@
+/*
+ * par2cuda — C ABI of the GB300 (sm_103a) PAR2 recovery backend.
+ *
+ * One handle = one backend instance on one CUDA device, the counterpart of a
+ * PAR2ProcOCL / PAR2ProcCPU object behind ParPar's backend plugin interface
+ * IPAR2ProcBackend (gf16/controller.h:77-217).  Each entry point below names
+ * the reference member it replaces.  A C++ adapter class deriving from
+ * IPAR2ProcBackend forwards its virtuals to these functions,
+ * so PAR2Proc (gf16/controller.cpp) and the node addon (src/gf.cc) drive it
+ * unchanged.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Host buffers may be pageable or pinned;
+ *    pinned (cudaHostAlloc / cudaHostRegister) buffers are copied directly.
+ *  - Return value: 0 = success, negative = error (the message is available
+ *    from par2cuda_last_error() on the calling thread).  The reference's
+ *    `bool false` results ("Failed to allocate memory", src/gf.cc:351-354)
+ *    map to a negative return.
+ *  - Completion callbacks run on a backend-owned thread, in submission order
+ *    per callback kind.  Under libuv the adapter re-posts them to the loop
+ *    with ThreadNotifyQueue (gf16/threadqueue.h), as the OpenCL backend does.
+ *  - Buffers passed to par2cuda_add_input are borrowed until its callback has
+ *    run (the reference's future/callback contract, gf16/controller_cpu.cpp:283-331).
+ *  - Output corruption is reported as valid = 0 in the get_output callback,
+ *    never as an error (gf16/controller_cpu.cpp:423-443, src/gf.cc:680-692).
+ *  - Slice sizes are byte counts of the current slice chunk: even, >= 2
+ *    (src/gf.cc:262, gf16/controller.cpp:76-78).
+ */
+#ifndef PAR2CUDA_H
+#define PAR2CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct par2cuda_ctx par2cuda_ctx;
+
+/* status / verdict callback: status >= 0 on success (get_output: 1 = checksum
+ * valid, 0 = invalid), negative on error */
+typedef void (*par2cuda_done_fn)(void* user, int status);
+/* batch-completion progress callback (IPAR2ProcBackend::progressCb,
+ * gf16/controller.h:93, called from _notifyProc gf16/controller_cpu.cpp:627-645) */
+typedef void (*par2cuda_progress_fn)(void* user, unsigned numInputs);
+
+/* canAdd() results — PAR2ProcBackendAddResult, gf16/controller.h:38-43 */
+enum { PAR2CUDA_ADD_OK = 0, PAR2CUDA_ADD_OK_BUSY = 1, PAR2CUDA_ADD_FULL = 2 };
+
+/* multiply-accumulate kernels (the Galois16OCLMethods analogue, gf16/controller_ocl.h:15-31) */
+enum {
+	PAR2CUDA_METHOD_AUTO = 0,
+	PAR2CUDA_METHOD_COMB = 1,   /* shared-memory XOR-combination tables (default) */
+	PAR2CUDA_METHOD_XOR = 2,    /* LOP3, per-coefficient-bit masks */
+	PAR2CUDA_METHOD_NIBBLE = 3  /* shared-memory split-nibble tables */
+};
+
+typedef struct par2cuda_info {
+	int device;
+	char device_name[128];
+	char method_desc[64];        /* GetInfo "method_desc" (src/gf.cc:527-568) */
+	unsigned staging_count;      /* "staging_count" */
+	unsigned staging_size;       /* "staging_size" = input batch size */
+	unsigned min_staging_size;
+	size_t chunk_size;           /* "chunk_size": bytes per kernel tile column (128) */
+	size_t slice_mem;            /* "slice_mem": device bytes per slice row (pitch) */
+	size_t slice_size;           /* current slice chunk size */
+	unsigned num_output_slices;  /* "num_output_slices" */
+	unsigned batches_started;    /* getBatchesStarted() gf16/controller.h:208-210 */
+	size_t device_bytes;         /* device memory held by this backend */
+} par2cuda_info;
+
+/* Library version string. */
+const char* par2cuda_version(void);
+/* Message of the last failed call on this thread. */
+const char* par2cuda_last_error(void);
+/* Number of visible CUDA devices (negative on error) — the getDevices()
+ * analogue of PAR2ProcOCL (gf16/controller_ocl.h:173). */
+int par2cuda_device_count(void);
+
+/* Constructor: PAR2ProcOCL(loop, platformId, deviceId, stagingAreas)
+ * gf16/controller_ocl.h:188; stagingAreas as parsed in src/gf.cc:326-330. */
+int par2cuda_create(int device, unsigned staging_areas, par2cuda_ctx** out);
+/* init(method, targetInputBatch, ...) gf16/controller_ocl.h:191 /
+ * PAR2ProcCPU::init gf16/controller_cpu.cpp:79-115.  input_batch = 0 picks a
+ * default from the slice size.  Call after par2cuda_set_slice_size. */
+int par2cuda_init(par2cuda_ctx* ctx, int method, unsigned input_batch);
+/* setSliceSize(size) gf16/controller.h:160 */
+int par2cuda_set_slice_size(par2cuda_ctx* ctx, size_t size);
+/* setCurrentSliceSize(size) gf16/controller.h:166 (chunked passes,
+ * gf16/controller.cpp:87-115, lib/par2.js:847-867) */
+int par2cuda_set_current_slice_size(par2cuda_ctx* ctx, size_t size);
+/* setRecoverySlices(numSlices, exponents) gf16/controller.h:167; exponents
+ * may be NULL when every input is added with explicit coefficients */
+int par2cuda_set_recovery_slices(par2cuda_ctx* ctx, unsigned num_slices, const uint16_t* exponents);
+/* setMinInputBatchSize(size) gf16/controller.h:212-214 */
+int par2cuda_set_min_input_batch(par2cuda_ctx* ctx, unsigned size);
+/* setProgressCb gf16/controller.h:162-164 */
+int par2cuda_set_progress_cb(par2cuda_ctx* ctx, par2cuda_progress_fn fn, void* user);
+
+/* canAdd() gf16/controller.h:168 -> PAR2CUDA_ADD_* (negative on error) */
+int par2cuda_can_add(par2cuda_ctx* ctx);
+/* waitForAdd() gf16/controller.h:194 (blocks until canAdd() != FULL) */
+int par2cuda_wait_for_add(par2cuda_ctx* ctx);
+/* addInput(buffer, size, inputNum, flush[, cb]) gf16/controller.h:169;
+ * size <= current slice size, shorter inputs are zero-padded;
+ * input_num 0..32767 (src/gf.cc:587).  cb(user, 0) once `buffer` is free. */
+int par2cuda_add_input(par2cuda_ctx* ctx, const void* buffer, size_t size, uint16_t input_num, int flush,
+                       par2cuda_done_fn cb, void* user);
+/* addInput(buffer, size, coeffs, flush[, cb]) gf16/controller.h:170;
+ * coeffs[r] = coefficient of this input for recovery slice r */
+int par2cuda_add_input_coeffs(par2cuda_ctx* ctx, const void* buffer, size_t size, const uint16_t* coeffs,
+                              int flush, par2cuda_done_fn cb, void* user);
+/* dummyInput(inputNum, flush) gf16/controller.h:171 (benchmarking: counts an
+ * input without transferring data) */
+int par2cuda_dummy_input(par2cuda_ctx* ctx, uint16_t input_num, int flush);
+/* fillInput(buffer) gf16/controller.h:172 (benchmarking: loads staging
+ * without computing); returns 1 once every staging area has been filled */
+int par2cuda_fill_input(par2cuda_ctx* ctx, const void* buffer);
+/* flush() gf16/controller.h:173 */
+int par2cuda_flush(par2cuda_ctx* ctx);
+/* endInput() gf16/controller.h:175-179: flushes, and cb(user, 0) runs once
+ * every batch has been processed (processing_finished, controller.h:192) */
+int par2cuda_end_input(par2cuda_ctx* ctx, par2cuda_done_fn cb, void* user);
+/* getOutput(index, output[, cb(valid)]) gf16/controller.h:185; `output`
+ * holds >= current slice size bytes (src/gf.cc:668-669) */
+int par2cuda_get_output(par2cuda_ctx* ctx, unsigned index, void* output, par2cuda_done_fn cb, void* user);
+/* discardOutput() gf16/controller.h:186-188: next batch overwrites */
+int par2cuda_discard_output(par2cuda_ctx* ctx);
+/* _hasAdded() gf16/controller.h:189-191 */
+int par2cuda_has_added(par2cuda_ctx* ctx);
+/* isEmpty() gf16/controller.h:182-184 */
+int par2cuda_is_empty(par2cuda_ctx* ctx);
+/* Blocks until every queued transfer, batch and callback has completed. */
+int par2cuda_sync(par2cuda_ctx* ctx);
+/* freeProcessingMem() gf16/controller.h:203 */
+int par2cuda_free_processing_mem(par2cuda_ctx* ctx);
+/* GfProc.info() fields, src/gf.cc:527-568 */
+int par2cuda_info_get(par2cuda_ctx* ctx, par2cuda_info* out);
+/* deinit() + destructor, gf16/controller.h:197-202 */
+int par2cuda_destroy(par2cuda_ctx* ctx);
+
+/* ---- device-level entry points (device pointers, caller's stream) ----
+ * The kernels of the backend above, for callers that keep slices resident
+ * on the GPU (the batched and serving paths).  `stream` is a cudaStream_t. */
+
+/* Bytes between rows the backend uses for a slice of `slice_bytes`: the data
+ * padded to 8 bytes, an 8-byte checksum block, rounded up to 128 bytes. */
+size_t par2cuda_row_pitch_bytes(size_t slice_bytes);
+/* Coefficient of input `input_num` for recovery exponent `exponent`
+ * (gfmat_coeff, gf16/gfmat_coeff.c:75-77). */
+uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent);
+/* Scratch bytes par2cuda_muladd needs for (num_rec, num_in). */
+size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in);
+/* rec[r][0..n_words) (^)= sum_i coeff[r*num_in + i] * in[i][0..n_words),
+ * the run_kernel body (gf16/controller_cpu.cpp:488-515).  Pitches are in
+ * 16-bit words (even); rows must be readable/writable up to
+ * roundup(n_words, 512) words (use par2cuda_row_pitch_bytes).
+ * accumulate = 0 overwrites rec (processingAdd false). */
+int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in,
+                    const uint16_t* d_coeff, uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec,
+                    size_t n_words, int accumulate, int method, void* d_scratch, size_t scratch_bytes,
+                    void* stream);
+/* Zero-pads rows past lens[i] bytes and writes the internal checksum block
+ * of each row (gf16_cksum_copy, gf16/gf16_cksum_base.h:32-46), or with
+ * verify = 1 compares it into d_flags[i] (gf16_cksum_copy_check :48-60).
+ * d_lens may be NULL (every row is slice_bytes long).  d_scratch: 8 bytes per row. */
+int par2cuda_rows_checksum(uint16_t* d_rows, size_t pitch_words, unsigned num_rows, const uint32_t* d_lens,
+                           size_t slice_bytes, int verify, uint8_t* d_flags, void* d_scratch, void* stream);
+/* Seeded synthetic bytes (same bytes as parpar_gb300/synth.py). */
+int par2cuda_synth_fill(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes,
+                        uint64_t seed, uint64_t first_index, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PAR2CUDA_H */

@@ -1,0 +1,168 @@
+// extern "C" entry points of include/par2cuda.h.
+#include "engine.h"
+
+#include <cstring>
+#include <new>
+
+namespace p2c { const uint16_t* host_input_logs(); }
+
+struct par2cuda_ctx {
+	p2c::Engine* eng;
+};
+
+#define P2C_CTX_CHECK(ctx) do { if(!(ctx) || !(ctx)->eng) { p2c::set_error("null handle"); return -1; } } while(0)
+
+extern "C" {
+
+const char* par2cuda_version(void) { return "par2cuda 0.1 (sm_103a)"; }
+const char* par2cuda_last_error(void) { return p2c::get_error(); }
+
+int par2cuda_device_count(void) {
+	int n = 0;
+	cudaError_t e = cudaGetDeviceCount(&n);
+	if(e != cudaSuccess) { p2c::set_error("cudaGetDeviceCount: %s", cudaGetErrorString(e)); return -1; }
+	return n;
+}
+
+int par2cuda_create(int device, unsigned staging_areas, par2cuda_ctx** out) {
+	if(!out) { p2c::set_error("null output handle"); return -1; }
+	*out = nullptr;
+	if(staging_areas < 1 || staging_areas > 32768) { p2c::set_error("staging area count %u is invalid", staging_areas); return -1; }
+	int n = par2cuda_device_count();
+	if(n < 0) return -1;
+	if(device < 0 || device >= n) { p2c::set_error("device %d not present (%d visible)", device, n); return -1; }
+	auto* ctx = new(std::nothrow) par2cuda_ctx;
+	if(!ctx) { p2c::set_error("out of host memory"); return -1; }
+	ctx->eng = new(std::nothrow) p2c::Engine(device, staging_areas);
+	if(!ctx->eng || ctx->eng->start()) {
+		delete ctx->eng;
+		delete ctx;
+		return -1;
+	}
+	*out = ctx;
+	return 0;
+}
+
+int par2cuda_init(par2cuda_ctx* ctx, int method, unsigned input_batch) {
+	P2C_CTX_CHECK(ctx);
+	return ctx->eng->init(method, input_batch);
+}
+int par2cuda_set_slice_size(par2cuda_ctx* ctx, size_t size) { P2C_CTX_CHECK(ctx); return ctx->eng->set_slice_size(size); }
+int par2cuda_set_current_slice_size(par2cuda_ctx* ctx, size_t size) { P2C_CTX_CHECK(ctx); return ctx->eng->set_current_slice_size(size); }
+int par2cuda_set_recovery_slices(par2cuda_ctx* ctx, unsigned n, const uint16_t* exps) {
+	P2C_CTX_CHECK(ctx);
+	if(n > 65534) { p2c::set_error("too many recovery slices (%u)", n); return -1; }
+	if(exps) for(unsigned i = 0; i < n; i++) if(exps[i] > 65534) { p2c::set_error("invalid recovery exponent %u", exps[i]); return -1; }
+	return ctx->eng->set_recovery_slices(n, exps);
+}
+int par2cuda_set_min_input_batch(par2cuda_ctx* ctx, unsigned size) { P2C_CTX_CHECK(ctx); ctx->eng->set_min_input_batch(size); return 0; }
+int par2cuda_set_progress_cb(par2cuda_ctx* ctx, par2cuda_progress_fn fn, void* user) { P2C_CTX_CHECK(ctx); ctx->eng->set_progress(fn, user); return 0; }
+int par2cuda_can_add(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->can_add(); }
+int par2cuda_wait_for_add(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->wait_for_add(); }
+int par2cuda_add_input(par2cuda_ctx* ctx, const void* buffer, size_t size, uint16_t input_num, int flush,
+                       par2cuda_done_fn cb, void* user) {
+	P2C_CTX_CHECK(ctx);
+	if(size && !buffer) { p2c::set_error("null input buffer"); return -1; }
+	return ctx->eng->add_input(buffer, size, input_num, nullptr, flush != 0, cb, user);
+}
+int par2cuda_add_input_coeffs(par2cuda_ctx* ctx, const void* buffer, size_t size, const uint16_t* coeffs, int flush,
+                              par2cuda_done_fn cb, void* user) {
+	P2C_CTX_CHECK(ctx);
+	if((size && !buffer) || !coeffs) { p2c::set_error("null input buffer or coefficients"); return -1; }
+	return ctx->eng->add_input(buffer, size, 0, coeffs, flush != 0, cb, user);
+}
+int par2cuda_dummy_input(par2cuda_ctx* ctx, uint16_t input_num, int flush) {
+	P2C_CTX_CHECK(ctx);
+	return ctx->eng->add_input(nullptr, 0, input_num, nullptr, flush != 0, nullptr, nullptr, true);
+}
+int par2cuda_fill_input(par2cuda_ctx* ctx, const void* buffer) { P2C_CTX_CHECK(ctx); return ctx->eng->fill_input(buffer); }
+int par2cuda_flush(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->flush(); }
+int par2cuda_end_input(par2cuda_ctx* ctx, par2cuda_done_fn cb, void* user) { P2C_CTX_CHECK(ctx); return ctx->eng->end_input(cb, user); }
+int par2cuda_get_output(par2cuda_ctx* ctx, unsigned index, void* output, par2cuda_done_fn cb, void* user) {
+	P2C_CTX_CHECK(ctx);
+	if(!output) { p2c::set_error("null output buffer"); return -1; }
+	return ctx->eng->get_output(index, output, cb, user);
+}
+int par2cuda_discard_output(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); ctx->eng->discard_output(); return 0; }
+int par2cuda_has_added(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->has_added() ? 1 : 0; }
+int par2cuda_is_empty(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->is_empty() ? 1 : 0; }
+int par2cuda_sync(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->sync(); }
+int par2cuda_free_processing_mem(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->free_processing_mem(); }
+int par2cuda_info_get(par2cuda_ctx* ctx, par2cuda_info* out) {
+	P2C_CTX_CHECK(ctx);
+	if(!out) { p2c::set_error("null info"); return -1; }
+	return ctx->eng->info(out);
+}
+int par2cuda_destroy(par2cuda_ctx* ctx) {
+	if(!ctx) return 0;
+	delete ctx->eng;
+	delete ctx;
+	return 0;
+}
+
+// ---------------------------------------------------------------- device level
+size_t par2cuda_row_pitch_bytes(size_t slice_bytes) { return p2c::row_pitch(slice_bytes) * 2; }
+
+uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent) {
+	const uint16_t* logs = p2c::host_input_logs();
+	uint32_t e = ((uint32_t)logs[input_num & 32767] * exponent) % 65535u;
+	uint32_t n = 1;
+	// 2^e by square-and-multiply in GF(2^16)
+	uint32_t b = 2;
+	while(e) {
+		if(e & 1) {
+			uint32_t p = 0, x = n;
+			for(int i = 0; i < 16; i++) { if(b >> i & 1) p ^= x; x <<= 1; if(x & 0x10000) x ^= P2C_POLY; }
+			n = p;
+		}
+		uint32_t p = 0, x = b;
+		for(int i = 0; i < 16; i++) { if(b >> i & 1) p ^= x; x <<= 1; if(x & 0x10000) x ^= P2C_POLY; }
+		b = p;
+		e >>= 1;
+	}
+	return (uint16_t)n;
+}
+
+size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in) {
+	return p2c::round_up(p2c::idx_bytes(num_rec, num_in), 256);
+}
+
+int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in, const uint16_t* d_coeff,
+                    uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec, size_t n_words, int accumulate,
+                    int method, void* d_scratch, size_t scratch_bytes, void* stream) {
+	cudaStream_t st = (cudaStream_t)stream;
+	if((in_pitch_words & 1) || (rec_pitch_words & 1)) { p2c::set_error("row pitches must be even (whole u32 pairs)"); return -1; }
+	if(method == PAR2CUDA_METHOD_XOR)
+		return p2c::xor_muladd(d_in, in_pitch_words, num_in, d_coeff, d_rec, rec_pitch_words, num_rec, n_words, accumulate, st);
+	if(method == PAR2CUDA_METHOD_NIBBLE) {
+		int dev = 0;
+		P2C_CUDA_TRY(cudaGetDevice(&dev));
+		p2c::GfTables gt;
+		if(p2c::gf_tables(dev, &gt)) return -1;
+		return p2c::nibble_muladd_t(d_in, in_pitch_words, num_in, d_coeff, d_rec, rec_pitch_words, num_rec, n_words, accumulate, gt, st);
+	}
+	if(method != PAR2CUDA_METHOD_AUTO && method != PAR2CUDA_METHOD_COMB) { p2c::set_error("unknown method %d", method); return -1; }
+	size_t need = par2cuda_muladd_scratch_bytes(num_rec, num_in);
+	if(scratch_bytes < need || (!d_scratch && need)) { p2c::set_error("scratch of %zu bytes needed, %zu given", need, scratch_bytes); return -1; }
+	uint4* idx = reinterpret_cast<uint4*>(d_scratch);
+	if(p2c::coeff_to_idx(d_coeff, num_rec, num_in, idx, st)) return -1;
+	return p2c::comb_muladd(d_in, in_pitch_words, num_in, idx, d_rec, rec_pitch_words, num_rec, n_words, accumulate, 0, st);
+}
+
+int par2cuda_rows_checksum(uint16_t* d_rows, size_t pitch_words, unsigned num_rows, const uint32_t* d_lens,
+                           size_t slice_bytes, int verify, uint8_t* d_flags, void* d_scratch, void* stream) {
+	int dev = 0;
+	P2C_CUDA_TRY(cudaGetDevice(&dev));
+	p2c::GfTables gt;
+	if(p2c::gf_tables(dev, &gt)) return -1;
+	if(verify && !d_flags) { p2c::set_error("verify needs d_flags"); return -1; }
+	return p2c::rows_cksum(d_rows, pitch_words, num_rows, d_lens, slice_bytes, (unsigned long long*)d_scratch,
+	                       verify, d_flags, gt, (cudaStream_t)stream);
+}
+
+int par2cuda_synth_fill(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes, uint64_t seed,
+                        uint64_t first_index, void* stream) {
+	return p2c::synth_fill(d_dst, pitch_bytes, num_rows, row_bytes, seed, first_index, (cudaStream_t)stream);
+}
+
+} // extern "C"

@@ -1,0 +1,187 @@
+// GF(2^16) multiply-accumulate of a batch of input rows into recovery rows:
+//     rec[r][w] (^)= sum_i c(r,i) * in[i][w]
+// (the hot loop of gf16/controller_cpu.cpp:488-515 / the OpenCL mul-group
+// kernel gf16/controller_ocl_init.cpp:588-671), as an XOR-combination-table
+// ("comb") kernel.
+//
+// Algebra.  Multiplication by c is linear over GF(2): with c = sum_k c_k x^k,
+//     sum_i c(r,i) in_i = sum_k x^k P[r][k],   P[r][k] = XOR_{i : bit k of c(r,i)} in_i
+// so the bulk of the work is 16 binary (XOR-only) combinations per recovery
+// row, followed by a 15-step Horner (multiply by x, XOR) per word at the end.
+// Inputs are taken 8 at a time: a CTA builds, in shared memory, the 256
+// possible XOR combinations T[m] = XOR_{t : bit t of m} in_{8g+t} of its word
+// tile, and each (recovery row, k) pair then costs one table row read:
+//     P[r][k] ^= T[ idx[r][g][k] ],  idx[r][g][k] = sum_t bit_k(c(r,8g+t)) << t
+// (the index bytes are prepared per launch by k_make_idx / k_coeff_to_idx).
+//
+// Roofline.  Per word mul-add the kernel reads 16/8 table entries of 2 bytes
+// from shared memory = 4 bytes, against the SM's 128 B/clk shared-memory
+// port: <= 32 word mul-adds / clk / SM.  HBM traffic per launch is
+// (nIn + 2R) rows; global index traffic is 2 bytes per (r, i) per word tile.
+//
+// Layout: CTA tile = 64 words (32 lanes x one u32 = 2 words) x RT recovery
+// rows (NW warps x RPW rows per warp); P accumulators live in registers
+// (16 u32 per row per lane).  Two table buffers interleave inside each
+// 256-byte table row (bytes 0-127 buffer 0, 128-255 buffer 1), so one PRMT
+// forms the full shared-memory address (m << 8 | buffer << 7 | lane << 2).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace p2c {
+
+template<int RPW, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) k_comb_muladd(
+	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
+	const uint4* __restrict__ idx, unsigned G,
+	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate)
+{
+	constexpr int RT = RPW * NW;              // recovery rows per CTA
+	constexpr int NB = NW >= 8 ? 8 : (NW >= 4 ? 4 : (NW >= 2 ? 2 : 1)); // build warps
+	constexpr int HPW = 16 / NB;             // high-nibble values built per build warp
+	extern __shared__ __align__(16) uint8_t smem[];
+	uint8_t* tbl = smem;                                    // 256 rows x 256 B
+	uint4* idxs = reinterpret_cast<uint4*>(smem + 65536);   // [2][RT]
+
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const size_t tile = blockIdx.x;
+	const unsigned rbase = blockIdx.y * RT;
+	const size_t colWord = tile * P2C_TILE_WORDS + lane * 2;  // this lane's 2 words
+	const uint32_t* in32 = reinterpret_cast<const uint32_t*>(in);
+
+	uint32_t acc[RPW][16];
+#pragma unroll
+	for(int s = 0; s < RPW; s++)
+#pragma unroll
+		for(int k = 0; k < 16; k++) acc[s][k] = 0;
+
+	// load the 8 input words of group g for this lane (zero past nIn)
+	auto load_group = [&](unsigned g, uint32_t (&x)[8]) {
+#pragma unroll
+		for(int t = 0; t < 8; t++) {
+			unsigned i = g * 8 + t;
+			x[t] = i < nIn ? __ldg(in32 + ((size_t)i * inPitch + colWord) / 2) : 0u;
+		}
+	};
+	// build table buffer `b` from x: rows (h << 4 | n), h in this warp's range
+	auto build = [&](int b, const uint32_t (&x)[8]) {
+		uint8_t* base = tbl + b * 128 + lane * 4;
+#pragma unroll
+		for(int hh = 0; hh < HPW; hh++) {
+			const int h = warp * HPW + hh;
+			uint32_t hv = 0;
+#pragma unroll
+			for(int t = 0; t < 4; t++) if(h >> t & 1) hv ^= x[4 + t];
+			uint32_t lv = hv;
+			uint8_t* rowp = base + h * 16 * 256;
+			*reinterpret_cast<uint32_t*>(rowp) = lv;       // n = 0
+#pragma unroll
+			for(int n = 1; n < 16; n++) {
+				const int gray = n ^ (n >> 1);
+				const int bit = (n & 1) ? 0 : (n & 2) ? 1 : (n & 4) ? 2 : 3;
+				lv ^= x[bit];
+				*reinterpret_cast<uint32_t*>(rowp + gray * 256) = lv;
+			}
+		}
+	};
+	auto stage_idx = [&](unsigned g, int b) {
+		for(int j = threadIdx.x; j < RT; j += NW * 32) {
+			unsigned r = rbase + j;
+			idxs[b * RT + j] = r < R ? __ldg(idx + (size_t)r * G + g) : make_uint4(0, 0, 0, 0);
+		}
+	};
+
+	uint32_t x[8];
+	if(warp < NB) { load_group(0, x); build(0, x); }
+	stage_idx(0, 0);
+	__syncthreads();
+
+	const uint32_t lw0 = (uint32_t)lane * 4, lw1 = lw0 + 128;
+	for(unsigned g = 0; g < G; g++) {
+		const int b = g & 1;
+		const bool more = g + 1 < G;
+		if(more && warp < NB) load_group(g + 1, x);
+		const uint32_t lw = b ? lw1 : lw0;
+		// lookups for group g
+#pragma unroll
+		for(int s = 0; s < RPW; s++) {
+			const int j = warp * RPW + s;
+			if(rbase + j < R) {
+				const uint4 q = idxs[b * RT + j];
+				const uint32_t qq[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+				for(int k = 0; k < 16; k++) {
+					// selector: byte0 <- lw.byte0, byte1 <- q.byte(k&3), bytes 2,3 <- lw.byte1 (=0)
+					const uint32_t sel = 4u | ((uint32_t)(k & 3) << 4) | (5u << 8) | (5u << 12);
+					const uint32_t addr = __byte_perm(qq[k >> 2], lw, sel);
+					acc[s][k] ^= *reinterpret_cast<const uint32_t*>(tbl + addr);
+				}
+			}
+		}
+		if(more) {
+			if(warp < NB) build(b ^ 1, x);
+			stage_idx(g + 1, b ^ 1);
+		}
+		__syncthreads();
+	}
+
+	// epilogue: rec[r] (^)= sum_k x^k P[r][k]
+	uint32_t* rec32 = reinterpret_cast<uint32_t*>(rec);
+#pragma unroll
+	for(int s = 0; s < RPW; s++) {
+		const unsigned r = rbase + warp * RPW + s;
+		if(r < R) {
+			uint32_t v = acc[s][15];
+#pragma unroll
+			for(int k = 14; k >= 0; k--) v = mul2x2(v) ^ acc[s][k];
+			uint32_t* p = rec32 + ((size_t)r * recPitch + colWord) / 2;
+			if(accumulate) v ^= *p;
+			*p = v;
+		}
+	}
+}
+
+template<int RPW, int NW>
+static int launch_comb(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec,
+                       size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st)
+{
+	constexpr int RT = RPW * NW;
+	const size_t smem = 65536 + 2 * RT * sizeof(uint4);
+	static bool attr = false;
+	if(!attr) {
+		P2C_CUDA_TRY(cudaFuncSetAttribute(k_comb_muladd<RPW, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		attr = true;
+	}
+	const unsigned G = (nIn + 7) / 8;
+	dim3 grid((unsigned)((nWords + P2C_TILE_WORDS - 1) / P2C_TILE_WORDS), (R + RT - 1) / RT);
+	k_comb_muladd<RPW, NW><<<grid, NW * 32, smem, st>>>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate);
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
+// Chooses the CTA shape from R: full 96-row blocks for large R, fewer warps /
+// rows per warp for small R so that little of a block is wasted.
+int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec, size_t recPitch,
+                unsigned R, size_t nWords, int accumulate, int shape, cudaStream_t st)
+{
+	if(!R || !nWords) return 0;
+	if(!nIn) {
+		if(!accumulate) P2C_CUDA_TRY(cudaMemset2DAsync(rec, recPitch * 2, 0, nWords * 2, R, st));
+		return 0;
+	}
+	if(shape <= 0) {
+		if(R <= 8) shape = 1;        // 1 warp x 8 rows
+		else if(R <= 32) shape = 2;  // 4 warps x 8 rows
+		else if(R <= 64) shape = 3;  // 8 warps x 8 rows
+		else shape = 4;              // 12 warps x 8 rows
+	}
+	switch(shape) {
+	case 1: return launch_comb<8, 1>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 2: return launch_comb<8, 4>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 3: return launch_comb<8, 8>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 5: return launch_comb<4, 16>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 6: return launch_comb<6, 12>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	default: return launch_comb<8, 12>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	}
+}
+
+} // namespace p2c

@@ -1,0 +1,39 @@
+// Host-side launchers of the device kernels (all asynchronous on `st`).
+#pragma once
+#include "common.cuh"
+
+namespace p2c {
+
+// device GF tables for `device` (built on first use, kept until exit)
+int gf_tables(int device, GfTables* out);
+
+// zero the bytes of each row at and past lens[row] (or sliceBytes when dLens is
+// null), compute the internal checksum over roundup(sliceBytes, 8) bytes and
+// either store it in the row's checksum block (verify = 0) or compare it with
+// the carried block into dFlags[row] (verify = 1).  dCkAcc: nRows x u64 scratch.
+int rows_cksum(uint16_t* rows, size_t pitchWords, unsigned nRows, const uint32_t* dLens, size_t sliceBytes,
+               unsigned long long* dCkAcc, int verify, uint8_t* dFlags, const GfTables& gt, cudaStream_t st);
+
+// index bytes for the comb kernel from PAR2 logs (dInLogs[nIn]) and recovery
+// exponents (dOutExp[R]) or from an explicit coefficient matrix
+// dCustom[nIn][R]; optionally also writes the coefficients [R][nIn]
+int make_idx(const uint16_t* dInLogs, const uint16_t* dCustom, const uint16_t* dOutExp, unsigned R, unsigned nIn,
+             uint4* dIdx, uint16_t* dCoeffOut, const GfTables& gt, cudaStream_t st);
+// index bytes from a coefficient matrix dCoeff[R][nIn]
+int coeff_to_idx(const uint16_t* dCoeff, unsigned R, unsigned nIn, uint4* dIdx, cudaStream_t st);
+inline size_t idx_bytes(unsigned R, unsigned nIn) { return (size_t)R * ((nIn + 7) / 8) * 16; }
+
+// rec[r][0..nWords) (^)= sum_i c(r,i) in[i][0..nWords), the comb kernel
+int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec, size_t recPitch,
+                unsigned R, size_t nWords, int accumulate, int shape, cudaStream_t st);
+
+// bit-sliced LOP3 kernel and split-nibble table kernel (same contract, coefficient matrix [R][nIn])
+int xor_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
+               size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st);
+int nibble_muladd_t(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
+                    size_t recPitch, unsigned R, size_t nWords, int accumulate, const GfTables& gt, cudaStream_t st);
+
+// seeded synthetic bytes (parpar_gb300/synth.py layout)
+int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first, cudaStream_t st);
+
+} // namespace p2c
