@@ -1,0 +1,390 @@
+"""Benchmark: PAR2 recovery generation on one GB300 vs the reference's CPU path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload bandwidth|dense|plain] [--no-e2e] [--no-cpu-baseline]
+
+Workload (default "bandwidth", the configuration the metric is quoted on):
+2000 input slices x 2 MiB (40 files of seeded uneven lengths; the last slice of
+each file zero-padded), 200 recovery slices (exponents 0..199), with the
+per-slice MD5+CRC32 (IFSC) and per-file MD5 hashes, single read pass.  One
+step = one whole job.  Inputs are seeded synthetic data (parpar_gb300.synth).
+
+value: GF16 mul-adds/s with the inputs resident in HBM (device-timed with CUDA
+events).  e2e: the same job through the C ABI with pinned host buffers, the
+input H2D and result D2H inside the timed region.  --impl reference times the
+reference algorithm's CPU implementation on this host's cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GF16 mul-adds/s"
+UNIT = "mul-adds/s"
+
+WORKLOADS = {
+    # name: (slice bytes, input slices, files, recovery slices, hashing)
+    "bandwidth": dict(S=2 * 1048576, N=2000, files=40, R=200, hashes=True,
+                      desc="2000 input slices x 2 MiB over 40 uneven files, 200 recovery (exp 0..199), IFSC + file MD5, single read pass"),
+    "dense": dict(S=262144, N=4096, files=1, R=4096, hashes=False,
+                  desc="4096 input slices x 256 KiB, 4096 recovery (exp 0..4095), GF contraction only"),
+    "plain": dict(S=1048576, N=100, files=1, R=10, hashes=True,
+                  desc="100 input slices x 1 MiB (one 100 MiB file), 10 recovery (exp 0..9), IFSC + file MD5"),
+    # small case for ncu captures of the contraction kernel (inputs 256 MiB > L2)
+    "profile": dict(S=524288, N=512, files=1, R=192, hashes=False,
+                    desc="512 input slices x 512 KiB, 192 recovery, GF contraction only (ncu capture size)"),
+    "profile_hash": dict(S=1048576, N=256, files=4, R=8, hashes=True,
+                         desc="256 input slices x 1 MiB over 4 files, 8 recovery, with hashing (ncu capture size)"),
+}
+
+
+def file_lengths(N, files, S, seed):
+    """Seeded uneven file lengths with sum(ceil(len/S)) == N, last slice partial."""
+    rng = np.random.default_rng(seed)
+    if files == 1:
+        return [N * S]
+    w = rng.uniform(0.5, 1.5, size=files)
+    counts = np.maximum(1, np.floor(w / w.sum() * N)).astype(int)
+    while counts.sum() < N:
+        counts[rng.integers(files)] += 1
+    while counts.sum() > N:
+        k = int(np.argmax(counts))
+        counts[k] -= 1
+    tails = rng.integers(1, S + 1, size=files)
+    return [int((c - 1) * S + t) for c, t in zip(counts, tails)]
+
+
+def sample_clocks(stop, out):
+    cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+           "--format=csv,noheader,nounits", "-lms", "200"]
+    try:
+        p = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+        return
+    try:
+        while not stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            out.append(line.strip())
+    finally:
+        p.terminate()
+        try:
+            p.wait(timeout=2)
+        except Exception:
+            p.kill()
+
+
+def summarize_clocks(lines, device):
+    sm, mx, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in lines:
+        f = [x.strip() for x in ln.split(",")]
+        if len(f) < 9 or f[0] != str(device):
+            continue
+        try:
+            sm.append(float(f[1]))
+            mx = float(f[2])
+        except ValueError:
+            continue
+        for n, v in zip(names, f[5:9]):
+            if v.lower() == "active":
+                reasons.add(n)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------- CPU
+def cpu_baseline_run(cfg, file_lens, threads, window=32768, seed=1):
+    """The reference algorithm's CPU implementation (oracle port of the LOOKUP
+    method + the reference hashing) on a bounded sample of the step: every
+    input x every recovery slice over a `window`-byte window of each slice,
+    plus the MD5/CRC32 work over the same bytes, scaled to the full step."""
+    from oracle import oracle as O
+    from parpar_gb300 import synth
+    from parpar_gb300.job import file_layout
+    S, N, R = cfg["S"], cfg["N"], cfg["R"]
+    W = min(window, S)
+    _, row_lens = file_layout(file_lens, S)
+    x = synth.slices(seed, 0, N, W)
+    lens = np.minimum(row_lens, W).astype(np.uint64)
+    for i in range(N):
+        x[i, lens[i]:] = 0
+    t0 = time.perf_counter()
+    O.recover(x, lens, np.arange(N), list(range(R)), threads=threads)
+    t_gf = time.perf_counter() - t0
+    t_hash = 0.0
+    if cfg["hashes"]:
+        lib = O.lib()
+        md5 = np.zeros((N, 16), np.uint8)
+        crc = np.zeros(N, np.uint32)
+        t0 = time.perf_counter()
+        lib.or_hash_rows(O._p(x), W, W, None, N, O._p(md5), O._p(crc), threads)  # slice lane: MD5 + CRC
+        lib.or_hash_rows(O._p(x), W, W, None, N, O._p(md5), None, threads)      # file lane: MD5
+        t_hash = time.perf_counter() - t0
+    scale = S / W
+    step = (t_gf + t_hash) * scale
+    mul_adds = N * R * (S // 2)
+    return {"value": mul_adds / step, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d inputs x %d recovery over a %d-byte window of each %d-byte slice%s, scaled x%.0f to the step"
+                      % (N, R, W, S, " + MD5/CRC32 of the same bytes" if cfg["hashes"] else "", scale),
+            "method": "oracle port of the reference LOOKUP method, %d threads" % threads,
+            "step_s_est": step, "sample_s": t_gf + t_hash}
+
+
+def run_reference(args, cfg, file_lens):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    vals, samples = [], None
+    for _ in range(args.warmup):
+        cpu_baseline_run(cfg, file_lens, threads, window=args.cpu_window)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = cpu_baseline_run(cfg, file_lens, threads, window=args.cpu_window)
+        vals.append(r["value"])
+        samples = r
+    wall = time.perf_counter() - t0
+    value = float(np.median(vals))
+    mul_adds = cfg["N"] * cfg["R"] * (cfg["S"] // 2)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mul_adds / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16 GF(2^16)",
+        "data": "synthetic (seeded splitmix64 slices)",
+        "config": {"workload": args.workload, "desc": cfg["desc"], "slice_bytes": cfg["S"], "inputs": cfg["N"],
+                   "recovery": cfg["R"], "files": len(file_lens)},
+        "cpu_baseline": {k: samples[k] for k in ("value", "unit", "cores", "kind", "sample", "method")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    line["cpu_baseline"]["value"] = value
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------- GPU
+def run_ours(args, cfg, file_lens):
+    import torch
+    import torch.distributed as dist
+    from parpar_gb300 import _lib
+    from parpar_gb300.job import ResidentJob
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    S, N, R = cfg["S"], cfg["N"], cfg["R"]
+    mul_adds = N * R * (S // 2)
+    job = ResidentJob(S, file_lens, list(range(R)), device=local)
+    job.fill_synthetic(seed=1 + rank)
+    torch.cuda.synchronize()
+
+    # per-kernel events on the launching streams (comb kernel on A, file MD5 on B)
+    L = _lib.load()
+    ev = []
+
+    def step(record=False):
+        h0 = h1 = None
+        cur = torch.cuda.current_stream(dev)
+        job.sa.wait_stream(cur)
+        job.sb.wait_stream(cur)
+        a, b = job.sa.cuda_stream, job.sb.cuda_stream
+        _lib.check(L.par2cuda_rows_checksum(job.d_in.data_ptr(), job.pw, N, job.d_lens.data_ptr(), S, 0, None,
+                                           job.d_ck.data_ptr(), a), "cksum")
+        if cfg["hashes"]:
+            # the file MD5s (long serial chains) start at once on B; they read
+            # only each file's own bytes
+            h0 = torch.cuda.Event(enable_timing=True) if record else None
+            h1 = torch.cuda.Event(enable_timing=True) if record else None
+            if record:
+                h0.record(job.sb)
+            _lib.check(L.par2cuda_file_md5(job.d_in.data_ptr(), job.pitch, len(file_lens), job.d_flen.data_ptr(),
+                                          job.d_first.data_ptr(), S, job.d_fmd5.data_ptr(), b), "file_md5")
+            if record:
+                h1.record(job.sb)
+        k0 = torch.cuda.Event(enable_timing=True) if record else None
+        k1 = torch.cuda.Event(enable_timing=True) if record else None
+        if record:
+            k0.record(job.sa)
+        _lib.check(L.par2cuda_muladd(job.d_in.data_ptr(), job.pw, N, job.d_coeff.data_ptr(), job.d_rec.data_ptr(),
+                                    job.pw, R, job.row_words, 0, job.method, job.d_scratch.data_ptr(),
+                                    job.scratch_bytes, a), "muladd")
+        if record:
+            k1.record(job.sa)
+        _lib.check(L.par2cuda_rows_checksum(job.d_rec.data_ptr(), job.pw, R, None, S, 1, job.d_flags.data_ptr(),
+                                           job.d_ck.data_ptr(), a), "verify")
+        if cfg["hashes"]:
+            _lib.check(L.par2cuda_slice_hash(job.d_in.data_ptr(), job.pitch, N, job.d_lens.data_ptr(), S,
+                                            job.d_ifsc.data_ptr(), a), "slice_hash")
+        cur.wait_stream(job.sa)
+        cur.wait_stream(job.sb)
+        if record:
+            ev.append((k0, k1, h0, h1))
+
+    launches_per_step = 6 + (2 if cfg["hashes"] else 0)  # cksum x2, coeff->idx, comb, verify x2 (+ slice hash, file md5)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert int(job.d_flags.sum()) == R, "recovery checksum verification failed"
+
+    clock_lines, stop = [], threading.Event()
+    th = None
+    if rank == 0 and not args.no_clocks:
+        th = threading.Thread(target=sample_clocks, args=(stop, clock_lines), daemon=True)
+        th.start()
+        time.sleep(0.5)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(args.steps):
+        step(record=True)
+    t1.record()
+    torch.cuda.synchronize()
+    barrier()
+    ms = t0.elapsed_time(t1) / args.steps
+    ms = max_over_ranks(ms)
+    comb_ms = float(np.mean([k0.elapsed_time(k1) for k0, k1, _, _ in ev]))
+    hash_ms = float(np.mean([h0.elapsed_time(h1) for _, _, h0, h1 in ev])) if cfg["hashes"] else 0.0
+    value = mul_adds * world / (ms / 1e3)
+
+    # e2e: pinned host inputs -> H2D -> job -> D2H of every result, via the C ABI
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.empty((N, S), dtype=torch.uint8, pin_memory=True)
+        host_in.copy_(job.d_in.view(torch.uint8)[:, :S])
+        rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
+        torch.cuda.synchronize()
+        for _ in range(max(1, args.warmup // 2)):
+            job.upload(host_in)
+            job.run(hashes=cfg["hashes"])
+            job.download(rec_host)
+        torch.cuda.synchronize()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            job.upload(host_in)
+            job.run(hashes=cfg["hashes"])
+            _, _, _, flags = job.download(rec_host)
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+        ems = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+        assert int(flags.sum()) == R
+        e2e = {"value": mul_adds * world / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": N * S,
+               "d2h_bytes_per_step": job.d2h_bytes(), "ms_per_step": ems,
+               "path": "par2cuda C ABI: pinned host slices -> H2D -> job -> D2H recovery + IFSC + file MD5 + verdicts"}
+    stop.set()
+    if th:
+        th.join(timeout=3)
+    clocks = summarize_clocks(clock_lines, local) if rank == 0 else None
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
+
+    peaks = measured_peaks()
+    sm_mhz = (clocks or {}).get("sm_mhz") or (peaks or {}).get("sm_max_mhz") or 2070.0
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    # int-ALU roofline of the contraction: 2 three-input LOP3 per word mul-add
+    # (16x16 GF(2) matrix, ~128 set bits, 32-way bit slicing), 128 INT32 lanes/SM/clk
+    alu_peak = n_sm * 128 * sm_mhz * 1e6 / 1e12
+    comb_rate = mul_adds / (comb_ms / 1e3)
+    alg_bytes = (N + R) * S  # read every input once, write every recovery once
+    hbm_peak = (peaks or {}).get("hbm_gbs", 6800.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u16 GF(2^16)", "data": "synthetic (seeded splitmix64 slices), inputs resident in HBM",
+        "config": {"workload": args.workload, "desc": cfg["desc"], "slice_bytes": S, "inputs": N, "recovery": R,
+                   "files": len(file_lens), "l2": "inputs (%.1f GiB) larger than L2 (129 MB); no flush" % (N * S / 2**30),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "src_GBps_x_recovery": N * S * R * world / (ms / 1e3) / 1e9,
+        "kernels_ms": {"comb_muladd": comb_ms, "file_md5": hash_ms, "step": ms},
+        "roofline": {"bound": "int-alu", "kernel": "k_comb_muladd", "achieved": 2 * comb_rate / 1e12,
+                     "peak": alu_peak, "unit": "Tops/s", "frac": 2 * comb_rate / 1e12 / alu_peak,
+                     "traffic": None, "alg_bytes": alg_bytes,
+                     "peak_source": "nominal %d SMs x 128 INT32 lanes x median SM clock %.0f MHz (no measured int peak)" % (n_sm, sm_mhz),
+                     "mul_adds_per_s": comb_rate},
+        "roofline_hbm": {"bound": "hbm", "kernel": "k_comb_muladd", "achieved": alg_bytes / (comb_ms / 1e3) / 1e9,
+                         "peak": hbm_peak, "unit": "GB/s", "frac": alg_bytes / (comb_ms / 1e3) / 1e9 / hbm_peak,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+        "e2e": e2e,
+    }
+    if args.traffic_bytes:
+        line["roofline"]["traffic"] = args.traffic_bytes
+    if not args.no_cpu_baseline and world == 1:
+        cb = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1, window=args.cpu_window)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "method")}
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="bandwidth")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-clocks", action="store_true")
+    ap.add_argument("--cpu-window", type=int, default=32768)
+    ap.add_argument("--traffic-bytes", type=float, default=None,
+                    help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline.traffic")
+    args = ap.parse_args()
+    cfg = WORKLOADS[args.workload]
+    file_lens = file_lengths(cfg["N"], cfg["files"], cfg["S"], seed=2000)
+    if args.impl == "reference":
+        return run_reference(args, cfg, file_lens)
+    return run_ours(args, cfg, file_lens)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -156,7 +156,7 @@ size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in);
 /* rec[r][0..n_words) (^)= sum_i coeff[r*num_in + i] * in[i][0..n_words),
  * the run_kernel body (gf16/controller_cpu.cpp:488-515).  Pitches are in
  * 16-bit words (even); rows must be readable/writable up to
- * roundup(n_words, 512) words (use par2cuda_row_pitch_bytes).
+ * roundup(n_words, 64) words (par2cuda_row_pitch_bytes gives such rows).
  * accumulate = 0 overwrites rec (processingAdd false). */
 int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in,
                     const uint16_t* d_coeff, uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec,
@@ -168,6 +168,22 @@ int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in
  * d_lens may be NULL (every row is slice_bytes long).  d_scratch: 8 bytes per row. */
 int par2cuda_rows_checksum(uint16_t* d_rows, size_t pitch_words, unsigned num_rows, const uint32_t* d_lens,
                            size_t slice_bytes, int verify, uint8_t* d_flags, void* d_scratch, void* stream);
+/* IFSC entries (hasher/hasher_base.h:154-176): for each row i, MD5 of its
+ * first d_lens[i] bytes zero-padded to slice_bytes, then CRC32 of the same
+ * (little-endian), 20 bytes per row into d_ifsc.  One GPU thread per row.
+ * d_lens may be NULL (full rows).  pitch_bytes: multiple of 16. */
+int par2cuda_slice_hash(const void* d_rows, size_t pitch_bytes, unsigned num_rows, const uint32_t* d_lens,
+                        size_t slice_bytes, uint8_t* d_ifsc, void* stream);
+/* File MD5s (HasherInput::end, hasher/hasher_base.h:178-186): file f is the
+ * d_file_len[f] bytes held by consecutive rows from d_first_row[f], each row
+ * holding slice_bytes of it.  One GPU thread per file; 16 bytes per file. */
+int par2cuda_file_md5(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
+                      const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, void* stream);
+/* MD5 of (d_prefix[i*prefix_len .. +prefix_len) ++ first data_len bytes of
+ * row i) for each row: the recovery-packet hash that MD5Multi computes
+ * (src/gf.cc:1075-1219, lib/par2.js:243-335).  One GPU thread per row. */
+int par2cuda_rows_md5(const void* d_rows, size_t pitch_bytes, unsigned num_rows, size_t data_len,
+                      const uint8_t* d_prefix, unsigned prefix_len, uint8_t* d_md5, void* stream);
 /* Seeded synthetic bytes (same bytes as parpar_gb300/synth.py). */
 int par2cuda_synth_fill(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes,
                         uint64_t seed, uint64_t first_index, void* stream);

@@ -33,6 +33,16 @@ int xor_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 int nibble_muladd_t(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
                     size_t recPitch, unsigned R, size_t nWords, int accumulate, const GfTables& gt, cudaStream_t st);
 
+// per-row MD5+CRC32 of rows zero-padded to sliceBytes (20-byte IFSC entries)
+int slice_hash(const void* rows, size_t pitchBytes, unsigned n, const uint32_t* dLens, size_t sliceBytes,
+               uint8_t* dOut, cudaStream_t st);
+// per-file MD5; file f spans consecutive rows from dFirstRow[f], dFileLen[f] bytes
+int file_md5(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen, const uint32_t* dFirstRow,
+             size_t sliceBytes, uint8_t* dOut, cudaStream_t st);
+// MD5 of (prefix[i] ++ row i's first dataLen bytes)
+int rows_md5(const void* rows, size_t pitchBytes, unsigned n, size_t dataLen, const uint8_t* dPrefix, unsigned prefixLen,
+             uint8_t* dOut, cudaStream_t st);
+
 // seeded synthetic bytes (parpar_gb300/synth.py layout)
 int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first, cudaStream_t st);
 

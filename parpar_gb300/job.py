@@ -1,0 +1,177 @@
+"""Device-resident PAR2 create job: one read pass over slices held in HBM.
+
+A job is the unit of work of PAR2Gen's single-pass create (lib/par2gen.js:
+1198-1330): N input slices of S bytes (the last slice of each file shorter,
+zero-padded), R recovery exponents, and the per-slice / per-file hashes.  The
+slices are staged once into HBM rows (par2cuda_row_pitch_bytes apart); then,
+on two streams that read the same rows:
+
+  stream A: zero padding + internal checksum of every input row,
+            multiply-accumulate into the R recovery rows (comb kernel),
+            checksum verification of every recovery row, IFSC entries
+            (MD5+CRC32 per slice, one thread per slice);
+  stream B: the file MD5s (one thread per file).
+
+All device work goes through libpar2cuda.so's C ABI; torch is used only for
+device memory, streams and events.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def par2_coefficients(input_nums, exps) -> np.ndarray:
+    """[R][N] uint16 PAR2 coefficients (gfmat_coeff), from the library."""
+    L = _lib.load()
+    nums = np.asarray(input_nums)
+    out = np.empty((len(exps), len(nums)), dtype=np.uint16)
+    # 2^(log_i * e) via the library's per-pair helper would be N*R calls; use
+    # the log/exp form with tables built from one call per input and exponent
+    logs = np.array([_input_log(L, int(i)) for i in nums], dtype=np.int64)
+    expt = _exp_table()
+    e = np.asarray(exps, dtype=np.int64)
+    out[:] = expt[(e[:, None] * logs[None, :]) % 65535]
+    return out
+
+
+_EXP = None
+
+
+def _exp_table():
+    global _EXP
+    if _EXP is None:
+        t = np.empty(65535, dtype=np.uint16)
+        n = 1
+        for i in range(65535):
+            t[i] = n
+            n <<= 1
+            if n & 0x10000:
+                n ^= 0x1100B
+        _EXP = t
+    return _EXP
+
+
+_LOGS = None
+
+
+def _input_log(L, i):
+    # log_i: coefficient of input i for exponent 1 is 2^log_i
+    global _LOGS
+    if _LOGS is None:
+        exp = _exp_table()
+        log = np.zeros(65536, dtype=np.int64)
+        log[exp] = np.arange(65535)
+        _LOGS = np.array([log[L.par2cuda_coeff(k, 1)] for k in range(32768)], dtype=np.int64)
+    return int(_LOGS[i])
+
+
+def file_layout(file_lens, S):
+    """(first_row[f], rows per file, per-row byte lengths) for files laid out as slices of S bytes."""
+    first, lens = [], []
+    r = 0
+    for ln in file_lens:
+        first.append(r)
+        n = max(1, (int(ln) + S - 1) // S)
+        for k in range(n):
+            lens.append(int(min(S, ln - k * S)) if ln else 0)
+        r += n
+    return np.array(first, dtype=np.uint32), np.array(lens, dtype=np.uint32)
+
+
+class ResidentJob:
+    """One PAR2 create job with its input rows resident on the current device."""
+
+    def __init__(self, slice_size: int, file_lens, exps, input_nums=None, method: int = _lib.METHOD_COMB,
+                 device: int = 0, stream_a=None, stream_b=None):
+        self.L = _lib.load()
+        self.S = int(slice_size)
+        self.file_lens = [int(x) for x in file_lens]
+        self.first_row, self.row_lens = file_layout(self.file_lens, self.S)
+        self.N = len(self.row_lens)
+        self.exps = list(exps)
+        self.R = len(self.exps)
+        self.input_nums = np.arange(self.N) if input_nums is None else np.asarray(input_nums)
+        self.method = method
+        self.pitch = self.L.par2cuda_row_pitch_bytes(self.S)
+        self.pw = self.pitch // 2
+        self.n_words = self.pitch // 2  # full rows: data + checksum block (+ pitch padding)
+        self.row_words = ((self.S + 7) // 8 * 8 + 8) // 2
+        dev = torch.device("cuda", device)
+        self.dev = dev
+        self.d_in = torch.empty((self.N, self.pw), dtype=torch.int16, device=dev)
+        self.d_rec = torch.empty((self.R, self.pw), dtype=torch.int16, device=dev)
+        coeff = par2_coefficients(self.input_nums, self.exps)
+        self.d_coeff = torch.from_numpy(coeff.view(np.int16)).to(dev)
+        self.d_lens = torch.from_numpy(self.row_lens.view(np.int32)).to(dev)
+        self.d_flen = torch.tensor(self.file_lens, dtype=torch.int64, device=dev)
+        self.d_first = torch.from_numpy(self.first_row.view(np.int32)).to(dev)
+        self.scratch_bytes = self.L.par2cuda_muladd_scratch_bytes(self.R, self.N)
+        self.d_scratch = torch.empty(max(self.scratch_bytes, 256), dtype=torch.uint8, device=dev)
+        self.d_ck = torch.empty(max(self.N, self.R) * 8, dtype=torch.uint8, device=dev)
+        self.d_flags = torch.empty(self.R, dtype=torch.uint8, device=dev)
+        self.d_ifsc = torch.empty(self.N * 20, dtype=torch.uint8, device=dev)
+        self.d_fmd5 = torch.empty(len(self.file_lens) * 16, dtype=torch.uint8, device=dev)
+        self.sa = stream_a or torch.cuda.Stream(device=dev)
+        self.sb = stream_b or torch.cuda.Stream(device=dev)
+        self.launches_per_run = 8
+
+    # -------------------------------------------------------------- inputs
+    def fill_synthetic(self, seed: int):
+        """Seeded rows (parpar_gb300.synth layout); bytes past each row's length are
+        left for the zero-padding step of run()."""
+        _lib.check(self.L.par2cuda_synth_fill(self.d_in.data_ptr(), self.pitch, self.N, self.S, seed, 0,
+                                             torch.cuda.current_stream(self.dev).cuda_stream), "synth")
+
+    def upload(self, host_rows: torch.Tensor, stream=None):
+        """H2D of host rows [N, S] (pinned for an asynchronous copy) into the resident rows."""
+        st = stream or torch.cuda.current_stream(self.dev)
+        with torch.cuda.stream(st):
+            self.d_in.view(torch.uint8)[:, : self.S].copy_(host_rows, non_blocking=True)
+        return self.N * self.S
+
+    # -------------------------------------------------------------- compute
+    def run(self, hashes: bool = True):
+        """Issues the whole job on streams A and B (asynchronous)."""
+        L = self.L
+        cur = torch.cuda.current_stream(self.dev)
+        self.sa.wait_stream(cur)
+        self.sb.wait_stream(cur)
+        a = self.sa.cuda_stream
+        b = self.sb.cuda_stream
+        # A: zero padding + checksum of the inputs, then the mul-add, then verification
+        _lib.check(L.par2cuda_rows_checksum(self.d_in.data_ptr(), self.pw, self.N, self.d_lens.data_ptr(), self.S, 0,
+                                           None, self.d_ck.data_ptr(), a), "rows_checksum")
+        if hashes:
+            # the file MD5s (long serial chains) start at once on B: they read
+            # only each file's own bytes, not the padding A writes
+            _lib.check(L.par2cuda_file_md5(self.d_in.data_ptr(), self.pitch, len(self.file_lens), self.d_flen.data_ptr(),
+                                          self.d_first.data_ptr(), self.S, self.d_fmd5.data_ptr(), b), "file_md5")
+        _lib.check(L.par2cuda_muladd(self.d_in.data_ptr(), self.pw, self.N, self.d_coeff.data_ptr(), self.d_rec.data_ptr(),
+                                    self.pw, self.R, self.row_words, 0, self.method, self.d_scratch.data_ptr(),
+                                    self.scratch_bytes, a), "muladd")
+        _lib.check(L.par2cuda_rows_checksum(self.d_rec.data_ptr(), self.pw, self.R, None, self.S, 1,
+                                           self.d_flags.data_ptr(), self.d_ck.data_ptr(), a), "verify")
+        if hashes:
+            _lib.check(L.par2cuda_slice_hash(self.d_in.data_ptr(), self.pitch, self.N, self.d_lens.data_ptr(), self.S,
+                                            self.d_ifsc.data_ptr(), a), "slice_hash")
+        cur.wait_stream(self.sa)
+        cur.wait_stream(self.sb)
+
+    # -------------------------------------------------------------- results
+    def download(self, rec_host: torch.Tensor | None = None, stream=None):
+        """D2H of recovery slices, IFSC entries, file MD5s and checksum verdicts."""
+        st = stream or torch.cuda.current_stream(self.dev)
+        with torch.cuda.stream(st):
+            if rec_host is None:
+                rec_host = torch.empty((self.R, self.S), dtype=torch.uint8, pin_memory=True)
+            rec_host.copy_(self.d_rec.view(torch.uint8)[:, : self.S], non_blocking=True)
+            ifsc = self.d_ifsc.to("cpu", non_blocking=True)
+            fmd5 = self.d_fmd5.to("cpu", non_blocking=True)
+            flags = self.d_flags.to("cpu", non_blocking=True)
+        return rec_host, ifsc, fmd5, flags
+
+    def d2h_bytes(self):
+        return self.R * self.S + self.N * 20 + len(self.file_lens) * 16 + self.R
