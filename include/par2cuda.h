@@ -162,6 +162,19 @@ int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in
                     const uint16_t* d_coeff, uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec,
                     size_t n_words, int accumulate, int method, void* d_scratch, size_t scratch_bytes,
                     void* stream);
+/* par2cuda_muladd with the comb method, for callers that cannot supply or
+ * allocate scratch memory (a fixed device-memory budget, or a submission loop
+ * that must not call cudaMalloc because an allocation may synchronise the
+ * device).  No counterpart in the reference.  The scratch is a 4 MiB array
+ * inside the library on each device that loads it, so it requires
+ * num_rec * ceil(num_in / 8) <= 262144 (larger calls are rejected with an
+ * error; split the inputs over several calls with accumulate = 1).  It
+ * allocates nothing.  The first call on a device looks up the array's address
+ * (make it before any stream capture).  All calls share the array: calls that
+ * overlap on the GPU race, so order them on one stream or with events. */
+int par2cuda_muladd_noalloc(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in,
+                            const uint16_t* d_coeff, uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec,
+                            size_t n_words, int accumulate, void* stream);
 /* Zero-pads rows past lens[i] bytes and writes the internal checksum block
  * of each row (gf16_cksum_copy, gf16/gf16_cksum_base.h:32-46), or with
  * verify = 1 compares it into d_flags[i] (gf16_cksum_copy_check :48-60).

@@ -69,6 +69,7 @@ SIGNATURES = [
     ("par2cuda_coeff", _u16, [_u16, _u16]),
     ("par2cuda_muladd_scratch_bytes", _sz, [_u, _u]),
     ("par2cuda_muladd", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _i, _vp, _sz, _vp]),
+    ("par2cuda_muladd_noalloc", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _vp]),
     ("par2cuda_rows_checksum", _i, [_vp, _sz, _u, _vp, _sz, _i, _vp, _vp, _vp]),
     ("par2cuda_slice_hash", _i, [_vp, _sz, _u, _vp, _sz, _vp, _vp]),
     ("par2cuda_file_md5", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _vp]),
