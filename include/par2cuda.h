@@ -105,7 +105,11 @@ int par2cuda_can_add(par2cuda_ctx* ctx);
 int par2cuda_wait_for_add(par2cuda_ctx* ctx);
 /* addInput(buffer, size, inputNum, flush[, cb]) gf16/controller.h:169;
  * size <= current slice size, shorter inputs are zero-padded;
- * input_num 0..32767 (src/gf.cc:587).  cb(user, 0) once `buffer` is free. */
+ * input_num 0..32767 (src/gf.cc:587).  cb(user, 0) once `buffer` is free.
+ * Returns 1 when this call submitted a batch (the controller's active batch
+ * count goes up; the progress callback fires when it completes), 0 otherwise.
+ * The same holds for par2cuda_add_input_coeffs, par2cuda_dummy_input and
+ * par2cuda_flush. */
 int par2cuda_add_input(par2cuda_ctx* ctx, const void* buffer, size_t size, uint16_t input_num, int flush,
                        par2cuda_done_fn cb, void* user);
 /* addInput(buffer, size, coeffs, flush[, cb]) gf16/controller.h:170;
@@ -151,6 +155,10 @@ size_t par2cuda_row_pitch_bytes(size_t slice_bytes);
 /* Coefficient of input `input_num` for recovery exponent `exponent`
  * (gfmat_coeff, gf16/gfmat_coeff.c:75-77). */
 uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent);
+/* CTA shape of the comb kernel for every later call in this process (the
+ * autotuner's knob): 0 = chosen from the number of recovery rows, 1..9 = a
+ * fixed (rows per warp x warps) shape.  Returns the previous setting. */
+int par2cuda_set_comb_shape(int shape);
 /* Scratch bytes par2cuda_muladd needs for (num_rec, num_in). */
 size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in);
 /* rec[r][0..n_words) (^)= sum_i coeff[r*num_in + i] * in[i][0..n_words),

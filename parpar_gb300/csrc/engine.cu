@@ -266,7 +266,7 @@ int Engine::add_input(const void* buf, size_t size, int inputNum, const uint16_t
 		if(++currentStagingArea == staging.size()) currentStagingArea = 0;
 	}
 	enqueue(rq);
-	return 0;
+	return submit ? 1 : 0;
 }
 
 int Engine::fill_input(const void* buf) {
@@ -296,11 +296,11 @@ int Engine::flush() {
 	currentStagingInputs = 0;
 	if(++currentStagingArea == staging.size()) currentStagingArea = 0;
 	enqueue(rq);
-	return 0;
+	return 1;
 }
 
 int Engine::end_input(par2cuda_done_fn cb, void* user) {
-	if(flush()) return -1;
+	if(flush() < 0) return -1;
 	Req rq{Req::END};
 	rq.cb = cb; rq.user = user;
 	enqueue(rq);

@@ -27,6 +27,8 @@
 #include "common.cuh"
 #include "kernels.h"
 
+#include <atomic>
+
 namespace p2c {
 
 template<int RPW, int NW>
@@ -36,8 +38,6 @@ __global__ void __launch_bounds__(NW * 32, 1) k_comb_muladd(
 	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate)
 {
 	constexpr int RT = RPW * NW;              // recovery rows per CTA
-	constexpr int NB = NW >= 8 ? 8 : (NW >= 4 ? 4 : (NW >= 2 ? 2 : 1)); // build warps
-	constexpr int HPW = 16 / NB;             // high-nibble values built per build warp
 	extern __shared__ __align__(16) uint8_t smem[];
 	uint8_t* tbl = smem;                                    // 256 rows x 256 B
 	uint4* idxs = reinterpret_cast<uint4*>(smem + 65536);   // [2][RT]
@@ -54,7 +54,9 @@ __global__ void __launch_bounds__(NW * 32, 1) k_comb_muladd(
 #pragma unroll
 		for(int k = 0; k < 16; k++) acc[s][k] = 0;
 
-	// load the 8 input words of group g for this lane (zero past nIn)
+	constexpr int NB = NW >= 8 ? 8 : (NW >= 4 ? 4 : (NW >= 2 ? 2 : 1)); // build warps
+	constexpr int HPW = 16 / NB;             // high-nibble values built per build warp
+	// the 8 input words of group g for this lane (zero past nIn)
 	auto load_group = [&](unsigned g, uint32_t (&x)[8]) {
 #pragma unroll
 		for(int t = 0; t < 8; t++) {
@@ -62,7 +64,9 @@ __global__ void __launch_bounds__(NW * 32, 1) k_comb_muladd(
 			x[t] = i < nIn ? __ldg(in32 + ((size_t)i * inPitch + colWord) / 2) : 0u;
 		}
 	};
-	// build table buffer `b` from x: rows (h << 4 | n), h in this warp's range
+	// build table buffer `b` from x (build warps only): rows (h << 4 | n) for
+	// this warp's HPW high nibbles h, the 16 low nibbles n in Gray-code order so
+	// that each row costs one XOR
 	auto build = [&](int b, const uint32_t (&x)[8]) {
 		uint8_t* base = tbl + b * 128 + lane * 4;
 #pragma unroll
@@ -146,17 +150,16 @@ static int launch_comb(const uint16_t* in, size_t inPitch, unsigned nIn, const u
 {
 	constexpr int RT = RPW * NW;
 	const size_t smem = 65536 + 2 * RT * sizeof(uint4);
-	static bool attr = false;
-	if(!attr) {
-		P2C_CUDA_TRY(cudaFuncSetAttribute(k_comb_muladd<RPW, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		attr = true;
-	}
+	P2C_CUDA_TRY(cudaFuncSetAttribute(k_comb_muladd<RPW, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const unsigned G = (nIn + 7) / 8;
 	dim3 grid((unsigned)((nWords + P2C_TILE_WORDS - 1) / P2C_TILE_WORDS), (R + RT - 1) / RT);
 	k_comb_muladd<RPW, NW><<<grid, NW * 32, smem, st>>>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate);
 	P2C_CUDA_TRY(cudaGetLastError());
 	return 0;
 }
+
+static std::atomic<int> g_comb_shape{0};
+int set_comb_shape(int shape) { return g_comb_shape.exchange(shape); }
 
 // Chooses the CTA shape from R: full 96-row blocks for large R, fewer warps /
 // rows per warp for small R so that little of a block is wasted.
@@ -168,6 +171,7 @@ int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* i
 		if(!accumulate) P2C_CUDA_TRY(cudaMemset2DAsync(rec, recPitch * 2, 0, nWords * 2, R, st));
 		return 0;
 	}
+	if(shape <= 0) shape = g_comb_shape.load();
 	if(shape <= 0) {
 		if(R <= 8) shape = 1;        // 1 warp x 8 rows
 		else if(R <= 32) shape = 2;  // 4 warps x 8 rows
@@ -178,8 +182,11 @@ int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* i
 	case 1: return launch_comb<8, 1>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 2: return launch_comb<8, 4>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 3: return launch_comb<8, 8>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
-	case 5: return launch_comb<4, 16>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
-	case 6: return launch_comb<6, 12>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 5: return launch_comb<4, 20>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 6: return launch_comb<6, 14>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 7: return launch_comb<5, 16>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 8: return launch_comb<4, 16>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 9: return launch_comb<2, 32>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	default: return launch_comb<8, 12>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	}
 }

@@ -27,6 +27,9 @@ inline size_t idx_bytes(unsigned R, unsigned nIn) { return (size_t)R * ((nIn + 7
 int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec, size_t recPitch,
                 unsigned R, size_t nWords, int accumulate, int shape, cudaStream_t st);
 
+// process-wide CTA shape override for the comb kernel (0 = choose from R); returns the previous value
+int set_comb_shape(int shape);
+
 // bit-sliced LOP3 kernel and split-nibble table kernel (same contract, coefficient matrix [R][nIn])
 int xor_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
                size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st);

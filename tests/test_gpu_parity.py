@@ -267,3 +267,29 @@ def test_large_shapes_sampled(n, R, S):
     torch.cuda.synchronize()
     assert int(flags.sum()) == R
     _sampled_check(torch, d_in, pw, n, d_rec, R, S, exps)
+
+
+@pytest.mark.parametrize("shape", list(range(0, 10)))
+def test_comb_every_cta_shape(shape):
+    """Every comb CTA shape (rows per warp x warps) gives the oracle's result,
+    including partial recovery blocks and a ragged input group."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    prev = L.par2cuda_set_comb_shape(shape)
+    try:
+        n, R, S = 43, 101, 3000
+        d_in, pw = _dev_rows(torch, n, S, 21 + shape)
+        host_in = synth.slices(21 + shape, 0, n, S)
+        rng = np.random.default_rng(shape)
+        coeff = rng.integers(0, 65536, size=(R, n), dtype=np.uint16)
+        d_coeff = torch.from_numpy(coeff.view(np.int16)).cuda()
+        d_rec = torch.zeros((R, pw), dtype=torch.int16, device="cuda")
+        sb = L.par2cuda_muladd_scratch_bytes(R, n)
+        scratch = torch.zeros(sb, dtype=torch.uint8, device="cuda")
+        _lib.check(L.par2cuda_muladd(d_in.data_ptr(), pw, n, d_coeff.data_ptr(), d_rec.data_ptr(), pw, R, S // 2, 0,
+                                     1, scratch.data_ptr(), sb, None), "muladd")
+        torch.cuda.synchronize()
+        got = d_rec.cpu().numpy().view(np.uint8)[:, :S]
+        assert np.array_equal(got, O.recover_coeffs(host_in, np.full(n, S), coeff))
+    finally:
+        L.par2cuda_set_comb_shape(prev)
