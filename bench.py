@@ -1,7 +1,7 @@
 """Benchmark: PAR2 recovery generation on one GB300 vs the reference's CPU path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload bandwidth|dense|plain] [--no-e2e] [--no-cpu-baseline]
+                    [--workload bandwidth|dense|plain|batched] [--no-e2e] [--no-cpu-baseline]
 
 Workload (default "bandwidth", the configuration the metric is quoted on):
 2000 input slices x 2 MiB (40 files of seeded uneven lengths; the last slice of
@@ -45,6 +45,10 @@ WORKLOADS = {
                     desc="512 input slices x 512 KiB, 192 recovery, GF contraction only (ncu capture size)"),
     "profile_hash": dict(S=1048576, N=256, files=4, R=8, hashes=True,
                          desc="256 input slices x 1 MiB over 4 files, 8 recovery, with hashing (ncu capture size)"),
+    # configs[3]: 64 uneven jobs, one persistent graph-captured launch per pass
+    "batched": dict(S=0, N=0, files=0, R=0, hashes=False, jobs=64,
+                    desc="64 PAR2 jobs: N log-uniform [10,5000], S uniform 64 KiB..8 MiB (4-byte steps), R 1-30% of N; "
+                         "byte-window passes under a 64 GiB HBM budget; persistent graph-captured comb launches vs per-job launches"),
 }
 
 
@@ -365,6 +369,63 @@ def run_ours(args, cfg, file_lens):
     return 0
 
 
+def run_batched_workload(args, cfg):
+    """configs[3]: the uneven 64-job mix, batched (graph replay) vs per-job launches."""
+    import torch
+    from parpar_gb300 import autotune
+    from parpar_gb300.batch import BatchRunner, make_job_mix
+    torch.cuda.set_device(0)
+    jobs = make_job_mix(cfg["jobs"], seed=4)
+    runner = BatchRunner(jobs, budget_bytes=args.budget_gib << 30)
+    mul_adds = runner.mul_adds
+    # per-job launches: each job's passes, then wait for the job
+    for _ in range(max(1, args.warmup // 3)):
+        runner.run_per_job()
+    t0 = time.perf_counter()
+    lat = runner.run_per_job()
+    t_job = time.perf_counter() - t0
+    assert runner.all_valid()
+    runner.capture()
+    for _ in range(args.warmup):
+        runner.run_batched()
+    torch.cuda.synchronize()
+    clock_lines, stop = [], threading.Event()
+    th = None
+    if not args.no_clocks:
+        th = threading.Thread(target=sample_clocks, args=(stop, clock_lines), daemon=True)
+        th.start()
+        time.sleep(0.5)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        runner.run_batched()
+    e1.record()
+    torch.cuda.synchronize()
+    stop.set()
+    if th:
+        th.join(timeout=3)
+    assert runner.all_valid()
+    ms = e0.elapsed_time(e1) / args.steps
+    line = {
+        "metric": METRIC, "value": mul_adds / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u16 GF(2^16)", "data": "synthetic (seeded per-job slices generated on the device per pass)",
+        "config": {"workload": "batched", "desc": cfg["desc"], "jobs": len(jobs), "passes": runner.P,
+                   "input_GB": sum(j.input_bytes for j in jobs) / 1e9, "mul_adds": mul_adds,
+                   "l2": "per-pass working set tens of GB, far above L2"},
+        "jobs_per_s": len(jobs) / (ms / 1e3),
+        "per_job_launch": {"jobs_per_s": len(jobs) / t_job, "s": t_job,
+                           "p50_job_s": float(np.percentile(lat, 50)), "p99_job_s": float(np.percentile(lat, 99))},
+        "speedup_vs_per_job_launch": (len(jobs) / (ms / 1e3)) / (len(jobs) / t_job),
+        "autotune": {str(k): v[0] for k, v in autotune.table().items()},
+        "gpu_launches": runner.launches_per_run() * args.steps,
+        "clocks": summarize_clocks(clock_lines, 0),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -376,10 +437,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--cpu-window", type=int, default=32768)
+    ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline.traffic")
     args = ap.parse_args()
     cfg = WORKLOADS[args.workload]
+    if args.workload == "batched":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "batched workload is reported against per-job launches of this backend"}))
+            return 0
+        return run_batched_workload(args, cfg)
     file_lens = file_lengths(cfg["N"], cfg["files"], cfg["S"], seed=2000)
     if args.impl == "reference":
         return run_reference(args, cfg, file_lens)

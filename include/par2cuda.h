@@ -208,6 +208,39 @@ int par2cuda_rows_md5(const void* d_rows, size_t pitch_bytes, unsigned num_rows,
 /* Seeded synthetic bytes (same bytes as parpar_gb300/synth.py). */
 int par2cuda_synth_fill(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes,
                         uint64_t seed, uint64_t first_index, void* stream);
+/* The same bytes for the window [byte_offset, byte_offset + row_bytes) of each
+ * row's stream (byte_offset a multiple of 8): slice data for chunked passes. */
+int par2cuda_synth_fill_at(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes,
+                           uint64_t seed, uint64_t first_index, uint64_t byte_offset, void* stream);
+
+/* ---- batched multiply-accumulate over many jobs (one persistent launch) ----
+ * The reference processes one PAR2 job per controller; a GPU is only busy
+ * when many jobs share it, so this entry point runs the multiply-accumulate of
+ * many jobs (each with its own inputs, coefficients and recovery rows) in one
+ * persistent launch.  A job's work is split into units of (64-word tile x
+ * recovery block); CTAs take units from *d_counter (reset by the call), largest
+ * job first when the array is sorted that way. */
+typedef struct par2cuda_batch_job {
+	const uint16_t* d_in;        /* input rows */
+	size_t in_pitch_words;
+	unsigned num_in;
+	const void* d_index;         /* index bytes from par2cuda_coeff_index */
+	uint16_t* d_rec;             /* recovery rows */
+	size_t rec_pitch_words;
+	unsigned num_rec;
+	int accumulate;
+	unsigned long long unit_base; /* sum of par2cuda_batch_units() of the jobs before it */
+} par2cuda_batch_job;
+/* Bytes of index data for a job (num_rec x ceil(num_in/8) x 16). */
+size_t par2cuda_coeff_index_bytes(unsigned num_rec, unsigned num_in);
+/* Index bytes of a job from its coefficient matrix d_coeff[num_rec][num_in]. */
+int par2cuda_coeff_index(const uint16_t* d_coeff, unsigned num_rec, unsigned num_in, void* d_index, void* stream);
+/* Work units of a job with num_rec rows of n_words words for CTA shape 1..4
+ * (8 x {1,4,8,12} recovery rows per unit). */
+unsigned long long par2cuda_batch_units(unsigned num_rec, size_t n_words, int shape);
+/* One persistent launch over d_jobs[0..num_jobs) (device array). */
+int par2cuda_batch_muladd(const par2cuda_batch_job* d_jobs, unsigned num_jobs, unsigned long long total_units,
+                          unsigned long long* d_counter, int shape, void* stream);
 
 #ifdef __cplusplus
 }

@@ -76,7 +76,23 @@ SIGNATURES = [
     ("par2cuda_file_md5", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _vp]),
     ("par2cuda_rows_md5", _i, [_vp, _sz, _u, _sz, _vp, _u, _vp, _vp]),
     ("par2cuda_synth_fill", _i, [_vp, _sz, _u, _sz, _u64, _u64, _vp]),
+    ("par2cuda_synth_fill_at", _i, [_vp, _sz, _u, _sz, _u64, _u64, _u64, _vp]),
+    ("par2cuda_coeff_index_bytes", _sz, [_u, _u]),
+    ("par2cuda_coeff_index", _i, [_vp, _u, _u, _vp, _vp]),
+    ("par2cuda_batch_units", ctypes.c_ulonglong, [_u, _sz, _i]),
+    ("par2cuda_batch_muladd", _i, [_vp, _u, ctypes.c_ulonglong, _vp, _i, _vp]),
 ]
+
+
+class BatchJob(ctypes.Structure):
+    """par2cuda_batch_job (include/par2cuda.h)."""
+    _fields_ = [
+        ("d_in", ctypes.c_void_p), ("in_pitch_words", ctypes.c_size_t), ("num_in", ctypes.c_uint),
+        ("d_index", ctypes.c_void_p),
+        ("d_rec", ctypes.c_void_p), ("rec_pitch_words", ctypes.c_size_t), ("num_rec", ctypes.c_uint),
+        ("accumulate", ctypes.c_int),
+        ("unit_base", ctypes.c_ulonglong),
+    ]
 
 _lib = None
 

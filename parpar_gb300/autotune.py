@@ -1,0 +1,81 @@
+"""Autotuner for the comb kernel's CTA shape (recovery rows per CTA).
+
+The comb kernel's cost per word mul-add depends on how many recovery rows one
+CTA serves (the 256-row XOR table is built once per 8 inputs and shared by
+those rows, while accumulator registers bound the rows per CTA).  For each
+bucket of recovery counts the tuner times the candidate shapes on a small
+resident problem with the real kernel and keeps the fastest; results are
+cached per device for the process.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+
+# shape id -> recovery rows per CTA (8 rows per warp x warps)
+SHAPES = {1: 8, 2: 32, 3: 64, 4: 96}
+BUCKETS = [8, 16, 32, 64, 96, 128, 192, 100000]
+
+_cache: dict = {}
+
+
+def _bucket(R: int) -> int:
+    for b in BUCKETS:
+        if R <= b:
+            return b
+    return BUCKETS[-1]
+
+
+def _time_shape(shape: int, R: int, n: int = 256, slice_bytes: int = 262144, reps: int = 3) -> float:
+    L = _lib.load()
+    pitch = L.par2cuda_row_pitch_bytes(slice_bytes)
+    pw = pitch // 2
+    d_in = torch.empty((n, pw), dtype=torch.int16, device="cuda")
+    _lib.check(L.par2cuda_synth_fill(d_in.data_ptr(), pitch, n, slice_bytes, 99, 0, None), "synth")
+    coeff = torch.from_numpy(np.random.default_rng(R).integers(0, 65536, size=(R, n), dtype=np.uint16).view(np.int16)).cuda()
+    d_rec = torch.empty((R, pw), dtype=torch.int16, device="cuda")
+    sb = L.par2cuda_muladd_scratch_bytes(R, n)
+    scratch = torch.empty(max(sb, 256), dtype=torch.uint8, device="cuda")
+    nw = ((slice_bytes + 7) // 8 * 8 + 8) // 2
+    prev = L.par2cuda_set_comb_shape(shape)
+    try:
+        def once():
+            _lib.check(L.par2cuda_muladd(d_in.data_ptr(), pw, n, coeff.data_ptr(), d_rec.data_ptr(), pw, R, nw, 0,
+                                         _lib.METHOD_COMB, scratch.data_ptr(), sb, None), "muladd")
+        once()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            once()
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+    finally:
+        L.par2cuda_set_comb_shape(prev)
+
+
+def best_shape(R: int) -> int:
+    """Fastest batched comb shape (1..4) for R recovery rows on this device."""
+    dev = torch.cuda.current_device()
+    key = (dev, _bucket(R))
+    if key not in _cache:
+        Rb = min(_bucket(R), 384)
+        times = {s: _time_shape(s, Rb) for s in SHAPES}
+        _cache[key] = min(times, key=times.get)
+        _cache[(dev, "times", key[1])] = times
+    return _cache[key]
+
+
+def table() -> dict:
+    """{recovery bucket: (best shape, {shape: ms})} measured so far."""
+    out = {}
+    for k, v in _cache.items():
+        if len(k) == 2 and k[1] != "times":
+            out[k[1]] = (v, _cache.get((k[0], "times", k[1])))
+    return out

@@ -1,6 +1,7 @@
 // extern "C" entry points of include/par2cuda.h.
 #include "engine.h"
 
+#include <cstddef>
 #include <cstring>
 #include <new>
 
@@ -181,6 +182,33 @@ int par2cuda_rows_md5(const void* d_rows, size_t pitch_bytes, unsigned num_rows,
 int par2cuda_synth_fill(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes, uint64_t seed,
                         uint64_t first_index, void* stream) {
 	return p2c::synth_fill(d_dst, pitch_bytes, num_rows, row_bytes, seed, first_index, (cudaStream_t)stream);
+}
+
+int par2cuda_synth_fill_at(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes, uint64_t seed,
+                           uint64_t first_index, uint64_t byte_offset, void* stream) {
+	return p2c::synth_fill(d_dst, pitch_bytes, num_rows, row_bytes, seed, first_index, (cudaStream_t)stream, byte_offset);
+}
+
+size_t par2cuda_coeff_index_bytes(unsigned num_rec, unsigned num_in) { return p2c::idx_bytes(num_rec, num_in); }
+
+int par2cuda_coeff_index(const uint16_t* d_coeff, unsigned num_rec, unsigned num_in, void* d_index, void* stream) {
+	return p2c::coeff_to_idx(d_coeff, num_rec, num_in, reinterpret_cast<uint4*>(d_index), (cudaStream_t)stream);
+}
+
+unsigned long long par2cuda_batch_units(unsigned num_rec, size_t n_words, int shape) {
+	if(shape < 1 || shape > 4) return 0;
+	return p2c::comb_units(num_rec, n_words, shape);
+}
+
+static_assert(sizeof(par2cuda_batch_job) == sizeof(p2c::BatchJob), "batch job layout");
+static_assert(offsetof(par2cuda_batch_job, unit_base) == offsetof(p2c::BatchJob, unitBase), "batch job layout");
+static_assert(offsetof(par2cuda_batch_job, d_rec) == offsetof(p2c::BatchJob, rec), "batch job layout");
+
+int par2cuda_batch_muladd(const par2cuda_batch_job* d_jobs, unsigned num_jobs, unsigned long long total_units,
+                          unsigned long long* d_counter, int shape, void* stream) {
+	if(!d_counter && total_units) { p2c::set_error("null work counter"); return -1; }
+	return p2c::comb_batched(reinterpret_cast<const p2c::BatchJob*>(d_jobs), num_jobs, total_units, d_counter, shape,
+	                         (cudaStream_t)stream);
 }
 
 } // extern "C"

@@ -31,20 +31,21 @@
 
 namespace p2c {
 
+// One work unit: word tile `tile` (64 words) x recovery rows [rbase, rbase+RT)
+// of one job, all of its inputs.  Ends with every thread past a barrier and no
+// shared memory in use, so a CTA may run units back to back.
 template<int RPW, int NW>
-__global__ void __launch_bounds__(NW * 32, 1) k_comb_muladd(
+__device__ __forceinline__ void comb_unit(
 	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
 	const uint4* __restrict__ idx, unsigned G,
-	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate)
+	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate,
+	size_t tile, unsigned rbase, uint8_t* smem)
 {
 	constexpr int RT = RPW * NW;              // recovery rows per CTA
-	extern __shared__ __align__(16) uint8_t smem[];
 	uint8_t* tbl = smem;                                    // 256 rows x 256 B
 	uint4* idxs = reinterpret_cast<uint4*>(smem + 65536);   // [2][RT]
 
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	const size_t tile = blockIdx.x;
-	const unsigned rbase = blockIdx.y * RT;
 	const size_t colWord = tile * P2C_TILE_WORDS + lane * 2;  // this lane's 2 words
 	const uint32_t* in32 = reinterpret_cast<const uint32_t*>(in);
 
@@ -145,6 +146,56 @@ __global__ void __launch_bounds__(NW * 32, 1) k_comb_muladd(
 }
 
 template<int RPW, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) k_comb_muladd(
+	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
+	const uint4* __restrict__ idx, unsigned G,
+	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate)
+{
+	extern __shared__ __align__(16) uint8_t smem[];
+	comb_unit<RPW, NW>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate, blockIdx.x, blockIdx.y * (RPW * NW), smem);
+}
+
+// Persistent batched form: a grid of one CTA per SM (x occupancy) takes work
+// units (job, word tile, recovery block) from a device counter until the
+// list is exhausted.  Jobs are laid out job-major, largest first, so the
+// largest units are handed out first and the tail is made of small ones.
+// The counter is an atomicAdd ticket; there is no waiting on other CTAs.
+template<int RPW, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) k_comb_batched(
+	const BatchJob* __restrict__ jobs, unsigned nJobs, unsigned long long totalUnits,
+	unsigned long long* __restrict__ counter)
+{
+	constexpr int RT = RPW * NW;
+	extern __shared__ __align__(16) uint8_t smem[];
+	__shared__ unsigned long long s_unit;
+	__shared__ unsigned s_job;
+	for(;;) {
+		if(threadIdx.x == 0) {
+			unsigned long long u = atomicAdd(counter, 1ull);
+			s_unit = u;
+			// last job whose first unit <= u (unitBase ascending)
+			unsigned lo = 0, hi = nJobs;
+			while(hi - lo > 1) {
+				unsigned mid = (lo + hi) >> 1;
+				if(jobs[mid].unitBase <= u) lo = mid; else hi = mid;
+			}
+			s_job = lo;
+		}
+		__syncthreads();
+		const unsigned long long u = s_unit;
+		if(u >= totalUnits) break;
+		const BatchJob& J = jobs[s_job];
+		const unsigned long long local = u - J.unitBase;
+		const unsigned rblocks = (J.R + RT - 1) / RT;
+		const size_t tile = (size_t)(local / rblocks);
+		const unsigned rb = (unsigned)(local % rblocks);
+		comb_unit<RPW, NW>(J.in, J.inPitch, J.nIn, J.idx, (J.nIn + 7) / 8, J.rec, J.recPitch, J.R, J.accumulate,
+		                   tile, rb * RT, smem);
+		__syncthreads(); // s_unit / s_job are rewritten next round
+	}
+}
+
+template<int RPW, int NW>
 static int launch_comb(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec,
                        size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st)
 {
@@ -188,6 +239,50 @@ int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* i
 	case 8: return launch_comb<4, 16>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 9: return launch_comb<2, 32>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	default: return launch_comb<8, 12>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	}
+}
+
+// units per job for a shape: word tiles x recovery blocks
+unsigned long long comb_units(unsigned R, size_t nWords, int shape) {
+	static const int rt[10] = {96, 8, 32, 64, 96, 80, 84, 80, 64, 64};
+	if(shape <= 0) shape = g_comb_shape.load();
+	if(shape <= 0) shape = R <= 8 ? 1 : R <= 32 ? 2 : R <= 64 ? 3 : 4;
+	const unsigned RT = rt[shape > 9 ? 0 : shape];
+	return (unsigned long long)((nWords + P2C_TILE_WORDS - 1) / P2C_TILE_WORDS) * ((R + RT - 1) / RT);
+}
+
+template<int RPW, int NW>
+static int launch_batched(const BatchJob* jobs, unsigned nJobs, unsigned long long totalUnits,
+                          unsigned long long* counter, int ctasPerSm, cudaStream_t st)
+{
+	constexpr int RT = RPW * NW;
+	const size_t smem = 65536 + 2 * RT * sizeof(uint4);
+	P2C_CUDA_TRY(cudaFuncSetAttribute(k_comb_batched<RPW, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	int dev = 0, sms = 0;
+	P2C_CUDA_TRY(cudaGetDevice(&dev));
+	P2C_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	int occ = 1;
+	P2C_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_comb_batched<RPW, NW>, NW * 32, smem));
+	if(ctasPerSm > 0 && ctasPerSm < occ) occ = ctasPerSm;
+	if(occ < 1) occ = 1;
+	unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)sms * occ, totalUnits);
+	if(!grid) return 0;
+	P2C_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+	k_comb_batched<RPW, NW><<<grid, NW * 32, smem, st>>>(jobs, nJobs, totalUnits, counter);
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
+int comb_batched(const BatchJob* dJobs, unsigned nJobs, unsigned long long totalUnits, unsigned long long* dCounter,
+                 int shape, cudaStream_t st)
+{
+	if(!nJobs || !totalUnits) return 0;
+	switch(shape) {
+	case 1: return launch_batched<8, 1>(dJobs, nJobs, totalUnits, dCounter, 0, st);
+	case 2: return launch_batched<8, 4>(dJobs, nJobs, totalUnits, dCounter, 0, st);
+	case 3: return launch_batched<8, 8>(dJobs, nJobs, totalUnits, dCounter, 0, st);
+	case 4: return launch_batched<8, 12>(dJobs, nJobs, totalUnits, dCounter, 0, st);
+	default: set_error("batched comb shape %d not available (1..4)", shape); return -1;
 	}
 }
 

@@ -198,13 +198,14 @@ __device__ __forceinline__ uint64_t splitmix_mix(uint64_t z) {
 	z ^= z >> 27; z *= 0x94D049BB133111EBull;
 	return z ^ (z >> 31);
 }
-__global__ void k_synth(uint8_t* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first)
+__global__ void k_synth(uint8_t* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first,
+                        uint64_t unitOffset)
 {
 	const size_t units = (rowBytes + 7) / 8;
 	const size_t total = units * nRows;
 	for(size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (size_t)gridDim.x * blockDim.x) {
 		size_t row = id / units, u = id % units;
-		uint64_t z = splitmix_mix(seed * 0xD1342543DE82EF95ull + (first + row) * 0x9E3779B97F4A7C15ull + u);
+		uint64_t z = splitmix_mix(seed * 0xD1342543DE82EF95ull + (first + row) * 0x9E3779B97F4A7C15ull + unitOffset + u);
 		uint8_t* p = dst + row * pitchBytes + u * 8;
 		if(u * 8 + 8 <= rowBytes && ((reinterpret_cast<uintptr_t>(p) & 7) == 0)) {
 			*reinterpret_cast<uint64_t*>(p) = z;
@@ -214,12 +215,14 @@ __global__ void k_synth(uint8_t* dst, size_t pitchBytes, unsigned nRows, size_t 
 	}
 }
 
-int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first, cudaStream_t st)
+int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first, cudaStream_t st,
+               uint64_t byteOffset)
 {
+	if(byteOffset % 8) { set_error("synthetic window offset must be a multiple of 8"); return -1; }
 	size_t total = (rowBytes + 7) / 8 * (size_t)nRows;
 	if(!total) return 0;
 	unsigned blocks = (unsigned)std::min<size_t>((total + 255) / 256, 152 * 32);
-	k_synth<<<blocks, 256, 0, st>>>((uint8_t*)dst, pitchBytes, nRows, rowBytes, seed, first);
+	k_synth<<<blocks, 256, 0, st>>>((uint8_t*)dst, pitchBytes, nRows, rowBytes, seed, first, byteOffset / 8);
 	P2C_CUDA_TRY(cudaGetLastError());
 	return 0;
 }

@@ -27,6 +27,19 @@ inline size_t idx_bytes(unsigned R, unsigned nIn) { return (size_t)R * ((nIn + 7
 int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec, size_t recPitch,
                 unsigned R, size_t nWords, int accumulate, int shape, cudaStream_t st);
 
+// one job of a batched multiply-accumulate (device-resident descriptor;
+// same layout as par2cuda_batch_job in include/par2cuda.h)
+struct BatchJob {
+	const uint16_t* in; size_t inPitch; unsigned nIn;
+	const uint4* idx;              // index bytes (k_coeff_to_idx layout)
+	uint16_t* rec; size_t recPitch; unsigned R;
+	int accumulate;
+	unsigned long long unitBase;   // first work unit of this job (ascending)
+};
+unsigned long long comb_units(unsigned R, size_t nWords, int shape);
+int comb_batched(const BatchJob* dJobs, unsigned nJobs, unsigned long long totalUnits, unsigned long long* dCounter,
+                 int shape, cudaStream_t st);
+
 // process-wide CTA shape override for the comb kernel (0 = choose from R); returns the previous value
 int set_comb_shape(int shape);
 
@@ -46,7 +59,9 @@ int file_md5(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_
 int rows_md5(const void* rows, size_t pitchBytes, unsigned n, size_t dataLen, const uint8_t* dPrefix, unsigned prefixLen,
              uint8_t* dOut, cudaStream_t st);
 
-// seeded synthetic bytes (parpar_gb300/synth.py layout)
-int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first, cudaStream_t st);
+// seeded synthetic bytes (parpar_gb300/synth.py layout); byteOffset (a
+// multiple of 8) selects a window of each row's byte stream
+int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first, cudaStream_t st,
+               uint64_t byteOffset = 0);
 
 } // namespace p2c
