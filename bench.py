@@ -1,7 +1,7 @@
 """Benchmark: PAR2 recovery generation on one GB300 vs the reference's CPU path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload bandwidth|dense|plain|batched] [--no-e2e] [--no-cpu-baseline]
+                    [--workload bandwidth|dense|plain|batched|serving] [--no-e2e] [--no-cpu-baseline]
 
 Workload (default "bandwidth", the configuration the metric is quoted on):
 2000 input slices x 2 MiB (40 files of seeded uneven lengths; the last slice of
@@ -45,6 +45,10 @@ WORKLOADS = {
                     desc="512 input slices x 512 KiB, 192 recovery, GF contraction only (ncu capture size)"),
     "profile_hash": dict(S=1048576, N=256, files=4, R=8, hashes=True,
                          desc="256 input slices x 1 MiB over 4 files, 8 recovery, with hashing (ncu capture size)"),
+    # configs[4]: Poisson requests, admitted by free HBM, continuous batching
+    "serving": dict(S=0, N=0, files=0, R=0, hashes=False, jobs=48,
+                    desc="Poisson requests (sizes as the 64-job mix) at 200/s and at a sub-saturation rate; admission by "
+                         "free HBM (<=150 GB), chunked when over budget; jobs/s and p50/p99 latency"),
     # configs[3]: 64 uneven jobs, one persistent graph-captured launch per pass
     "batched": dict(S=0, N=0, files=0, R=0, hashes=False, jobs=64,
                     desc="64 PAR2 jobs: N log-uniform [10,5000], S uniform 64 KiB..8 MiB (4-byte steps), R 1-30% of N; "
@@ -369,6 +373,40 @@ def run_ours(args, cfg, file_lens):
     return 0
 
 
+def run_serving_workload(args, cfg):
+    """configs[4]: Poisson arrivals at 200/s (offered load above the GPU's
+    capacity) and at a sub-saturation rate; latency = completion - arrival."""
+    import torch
+    from parpar_gb300 import autotune
+    from parpar_gb300.serve import Server, make_requests, serve_stats
+    torch.cuda.set_device(0)
+    autotune.warm()
+    out = {}
+    for label, rate, n in (("offered_200_per_s", 200.0, cfg["jobs"]), ("sub_saturation_4_per_s", 4.0, cfg["jobs"] // 2)):
+        reqs = make_requests(n, rate, seed=5)
+        srv = Server(budget_bytes=150 * 10**9, slots=8)
+        t0 = time.perf_counter()
+        done = srv.run(reqs)
+        wall = time.perf_counter() - t0
+        st = serve_stats(done)
+        st["rate_per_s"] = rate
+        st["wall_s"] = wall
+        st["gpu_launches"] = srv.launches
+        out[label] = st
+    sat = out["offered_200_per_s"]
+    line = {
+        "metric": METRIC, "value": sat["mul_adds_per_s"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": sat["span_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u16 GF(2^16)", "data": "synthetic (seeded per-request slices generated on the device)",
+        "config": {"workload": "serving", "desc": cfg["desc"], "jobs": cfg["jobs"], "budget_GB": 150, "slots": 8},
+        "jobs_per_s": sat["jobs_per_s"], "p50_latency_s": sat["p50_latency_s"], "p99_latency_s": sat["p99_latency_s"],
+        "rates": out, "autotune": {str(k): v[0] for k, v in autotune.table().items()},
+        "gpu_launches": sat["gpu_launches"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_batched_workload(args, cfg):
     """configs[3]: the uneven 64-job mix, batched (graph replay) vs per-job launches."""
     import torch
@@ -442,11 +480,11 @@ def main():
                     help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline.traffic")
     args = ap.parse_args()
     cfg = WORKLOADS[args.workload]
-    if args.workload == "batched":
+    if args.workload in ("batched", "serving"):
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "batched workload is reported against per-job launches of this backend"}))
+            print(json.dumps({"impl": "reference", "unavailable": "the %s workload is reported against this backend's per-job path" % args.workload}))
             return 0
-        return run_batched_workload(args, cfg)
+        return run_batched_workload(args, cfg) if args.workload == "batched" else run_serving_workload(args, cfg)
     file_lens = file_lengths(cfg["N"], cfg["files"], cfg["S"], seed=2000)
     if args.impl == "reference":
         return run_reference(args, cfg, file_lens)

@@ -235,6 +235,11 @@ typedef struct par2cuda_batch_job {
 size_t par2cuda_coeff_index_bytes(unsigned num_rec, unsigned num_in);
 /* Index bytes of a job from its coefficient matrix d_coeff[num_rec][num_in]. */
 int par2cuda_coeff_index(const uint16_t* d_coeff, unsigned num_rec, unsigned num_in, void* d_index, void* stream);
+/* Index bytes of a PAR2 job computed on the device from its input numbers
+ * d_input_nums[num_in] and recovery exponents d_exponents[num_rec]
+ * (set_coeffs, gf16/controller_cpu.cpp:372-379, without a host matrix). */
+int par2cuda_par2_index(const uint16_t* d_input_nums, unsigned num_in, const uint16_t* d_exponents, unsigned num_rec,
+                        void* d_index, void* stream);
 /* Work units of a job with num_rec rows of n_words words for CTA shape 1..4
  * (8 x {1,4,8,12} recovery rows per unit). */
 unsigned long long par2cuda_batch_units(unsigned num_rec, size_t n_words, int shape);

@@ -79,6 +79,7 @@ SIGNATURES = [
     ("par2cuda_synth_fill_at", _i, [_vp, _sz, _u, _sz, _u64, _u64, _u64, _vp]),
     ("par2cuda_coeff_index_bytes", _sz, [_u, _u]),
     ("par2cuda_coeff_index", _i, [_vp, _u, _u, _vp, _vp]),
+    ("par2cuda_par2_index", _i, [_vp, _u, _vp, _u, _vp, _vp]),
     ("par2cuda_batch_units", ctypes.c_ulonglong, [_u, _sz, _i]),
     ("par2cuda_batch_muladd", _i, [_vp, _u, ctypes.c_ulonglong, _vp, _i, _vp]),
 ]

@@ -72,6 +72,12 @@ def best_shape(R: int) -> int:
     return _cache[key]
 
 
+def warm():
+    """Measures every bucket up front (a serving loop must not stop to tune)."""
+    for b in BUCKETS:
+        best_shape(min(b, 384))
+
+
 def table() -> dict:
     """{recovery bucket: (best shape, {shape: ms})} measured so far."""
     out = {}

@@ -165,6 +165,37 @@ int make_idx(const uint16_t* dInLogs, const uint16_t* dCustom, const uint16_t* d
 	return 0;
 }
 
+// PAR2 coefficients straight from input numbers and exponents -> index layout
+// (no host coefficient matrix: c = 2^(log(num_i) * e_r mod 65535))
+__global__ void k_par2_idx(const uint16_t* nums, const uint16_t* outExp, unsigned R, unsigned nIn, unsigned G, uint4* idx,
+                           GfTables gt)
+{
+	const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if(id >= (size_t)R * G) return;
+	const unsigned r = (unsigned)(id / G), g = (unsigned)(id % G);
+	const uint32_t e = outExp[r];
+	uint32_t q[4] = {0, 0, 0, 0};
+#pragma unroll
+	for(int t = 0; t < 8; t++) {
+		unsigned i = g * 8 + t;
+		uint32_t c = i < nIn ? gt.exp[((uint32_t)gt.inLog[nums[i] & 32767] * e) % 65535u] : 0;
+#pragma unroll
+		for(int k = 0; k < 16; k++) q[k >> 2] |= ((c >> k) & 1u) << (8 * (k & 3) + t);
+	}
+	idx[(size_t)r * G + g] = make_uint4(q[0], q[1], q[2], q[3]);
+}
+
+int par2_idx(const uint16_t* dNums, const uint16_t* dExp, unsigned R, unsigned nIn, uint4* dIdx, const GfTables& gt,
+             cudaStream_t st)
+{
+	unsigned G = (nIn + 7) / 8;
+	size_t n = (size_t)R * G;
+	if(!n) return 0;
+	k_par2_idx<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dNums, dExp, R, nIn, G, dIdx, gt);
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
 // coefficient matrix [R][nIn] -> index layout (used by the device-level entry point)
 __global__ void k_coeff_to_idx(const uint16_t* coeff, unsigned R, unsigned nIn, unsigned G, uint4* idx)
 {

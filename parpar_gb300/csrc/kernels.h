@@ -21,6 +21,9 @@ int make_idx(const uint16_t* dInLogs, const uint16_t* dCustom, const uint16_t* d
              uint4* dIdx, uint16_t* dCoeffOut, const GfTables& gt, cudaStream_t st);
 // index bytes from a coefficient matrix dCoeff[R][nIn]
 int coeff_to_idx(const uint16_t* dCoeff, unsigned R, unsigned nIn, uint4* dIdx, cudaStream_t st);
+// index bytes of PAR2 coefficients from input numbers dNums[nIn] and exponents dExp[R]
+int par2_idx(const uint16_t* dNums, const uint16_t* dExp, unsigned R, unsigned nIn, uint4* dIdx, const GfTables& gt,
+             cudaStream_t st);
 inline size_t idx_bytes(unsigned R, unsigned nIn) { return (size_t)R * ((nIn + 7) / 8) * 16; }
 
 // rec[r][0..nWords) (^)= sum_i c(r,i) in[i][0..nWords), the comb kernel
