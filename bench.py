@@ -43,6 +43,8 @@ WORKLOADS = {
     # small case for ncu captures of the contraction kernel (inputs 256 MiB > L2)
     "profile": dict(S=524288, N=512, files=1, R=192, hashes=False,
                     desc="512 input slices x 512 KiB, 192 recovery, GF contraction only (ncu capture size)"),
+    "profile_ws": dict(S=524288, N=512, files=1, R=200, hashes=False,
+                       desc="512 input slices x 512 KiB, 200 recovery, GF contraction only (ncu capture size, 72-row CTAs)"),
     "profile_hash": dict(S=1048576, N=256, files=4, R=8, hashes=True,
                          desc="256 input slices x 1 MiB over 4 files, 8 recovery, with hashing (ncu capture size)"),
     # configs[4]: Poisson requests, admitted by free HBM, continuous batching

@@ -157,8 +157,13 @@ size_t par2cuda_row_pitch_bytes(size_t slice_bytes);
 uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent);
 /* CTA shape of the comb kernel for every later call in this process (the
  * autotuner's knob): 0 = chosen from the number of recovery rows, 1..9 = a
- * fixed (rows per warp x warps) shape.  Returns the previous setting. */
+ * fixed (rows per warp x warps) shape; 10..15 = warp-specialised shapes
+ * (4 table-building warps + 8 or 12 lookup warps, 2 or 4 words per lane).  Returns the previous setting. */
 int par2cuda_set_comb_shape(int shape);
+/* Reads and clears the device-side error flag of the multiply-accumulate
+ * kernels: 1 when a bounded wait inside a kernel gave up (its results are then
+ * invalid), 0 otherwise, negative if the flag could not be read. */
+int par2cuda_device_error(void);
 /* Scratch bytes par2cuda_muladd needs for (num_rec, num_in). */
 size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in);
 /* rec[r][0..n_words) (^)= sum_i coeff[r*num_in + i] * in[i][0..n_words),

@@ -68,6 +68,7 @@ SIGNATURES = [
     ("par2cuda_row_pitch_bytes", _sz, [_sz]),
     ("par2cuda_coeff", _u16, [_u16, _u16]),
     ("par2cuda_set_comb_shape", _i, [_i]),
+    ("par2cuda_device_error", _i, []),
     ("par2cuda_muladd_scratch_bytes", _sz, [_u, _u]),
     ("par2cuda_muladd", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _i, _vp, _sz, _vp]),
     ("par2cuda_muladd_noalloc", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _vp]),

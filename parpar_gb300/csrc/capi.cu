@@ -125,9 +125,11 @@ uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent) {
 }
 
 int par2cuda_set_comb_shape(int shape) {
-	if(shape < 0 || shape > 9) { p2c::set_error("comb shape %d out of range 0..9", shape); return -1; }
+	if(shape < 0 || shape > 15) { p2c::set_error("comb shape %d out of range 0..15", shape); return -1; }
 	return p2c::set_comb_shape(shape);
 }
+
+int par2cuda_device_error(void) { return p2c::comb_error_take(); }
 
 size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in) {
 	return p2c::round_up(p2c::idx_bytes(num_rec, num_in), 256);

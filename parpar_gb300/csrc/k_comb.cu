@@ -209,8 +209,245 @@ static int launch_comb(const uint16_t* in, size_t inPitch, unsigned nIn, const u
 	return 0;
 }
 
+
+// ---------------------------------------------------------------------------
+// Warp-specialised form: 4 builder warps produce the XOR tables (and stage the
+// index bytes) into a two-buffer ring; NL lookup warps consume them.  Each
+// buffer has a "full" mbarrier (128 builder arrivals) and an "empty" mbarrier
+// (one arrival per lookup warp), so lookup warps never wait for one another,
+// only for a table that is not built yet.  Every wait is bounded: after
+// P2C_WAIT_LIMIT polls the kernel records an error in g_comb_error and the
+// thread leaves (the host reports it; nothing spins forever).
+#define P2C_WAIT_LIMIT (1u << 22)
+__device__ unsigned g_comb_error;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" :: "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+	const unsigned a = smem_addr(bar);
+	for(unsigned i = 0; i < P2C_WAIT_LIMIT; i++) {
+		unsigned ok;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+		if(ok) return true;
+	}
+	atomicExch(&g_comb_error, 1u);
+	return false;
+}
+
+// WIDE = 1: each lane owns 4 words (LDS.64 per lookup, 128-word tiles,
+// 512-byte table rows holding both buffers); WIDE = 0: 2 words (LDS.32,
+// 64-word tiles, 256-byte rows).  ASMLD issues the table reads as explicit
+// ld.shared with a 32-bit shared-window address.
+template<int RPW, int NL, int WIDE, bool ASMLD>
+__global__ void __launch_bounds__((NL + 4) * 32, 1) k_comb_ws(
+	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
+	const uint4* __restrict__ idx, unsigned G,
+	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate, size_t limitWords)
+{
+	constexpr int RT = RPW * NL;
+	constexpr int V = WIDE ? 2 : 1;                 // u32 per lane
+	constexpr int TW = P2C_TILE_WORDS * V;          // words per tile
+	constexpr int ROWB = 256 * V;                   // table row stride (both buffers)
+	constexpr int TBL = 256 * ROWB;
+	extern __shared__ __align__(16) uint8_t smem[];
+	uint8_t* tbl = smem;
+	uint4* idxs = reinterpret_cast<uint4*>(smem + TBL);           // [2][RT]
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TBL + 2 * RT * sizeof(uint4)); // full[2], empty[2]
+	const unsigned sbase = smem_addr(smem);
+
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const size_t tile = blockIdx.x;
+	const unsigned rbase = blockIdx.y * RT;
+	const size_t colWord = tile * TW + lane * 2 * V;
+	// rows are only guaranteed up to roundup(nWords, 64) words: with 128-word
+	// tiles the upper half of the last tile may lie beyond the row
+	const bool laneIn = colWord + 2 * V <= limitWords;
+
+	if(threadIdx.x == 0) {
+		mbar_init(&bars[0], 128);
+		mbar_init(&bars[1], 128);
+		mbar_init(&bars[2], NL);
+		mbar_init(&bars[3], NL);
+	}
+	__syncthreads();
+
+	if(warp >= NL) {
+		// ---------------- builders: 4 warps, 4 high nibbles each
+		const int bw = warp - NL;
+		const int bt = threadIdx.x - NL * 32; // 0..127
+		for(unsigned g = 0; g < G; g++) {
+			const int b = g & 1;
+			if(g >= 2 && !mbar_wait(&bars[2 + b], ((g >> 1) - 1) & 1)) return;
+			uint32_t x[8][V];
+#pragma unroll
+			for(int t = 0; t < 8; t++) {
+				unsigned i = g * 8 + t;
+				if(WIDE) {
+					uint2 v = (i < nIn && laneIn) ? __ldg(reinterpret_cast<const uint2*>(in + (size_t)i * inPitch + colWord)) : make_uint2(0, 0);
+					x[t][0] = v.x; x[t][V - 1] = v.y;
+				} else {
+					x[t][0] = i < nIn ? __ldg(reinterpret_cast<const uint32_t*>(in + (size_t)i * inPitch + colWord)) : 0u;
+				}
+			}
+			uint8_t* base = tbl + b * (ROWB / 2) + lane * 4 * V;
+#pragma unroll
+			for(int hh = 0; hh < 4; hh++) {
+				const int h = bw * 4 + hh;
+				uint32_t v[V];
+#pragma unroll
+				for(int c = 0; c < V; c++) {
+					v[c] = 0;
+#pragma unroll
+					for(int t = 0; t < 4; t++) if(h >> t & 1) v[c] ^= x[4 + t][c];
+				}
+				uint8_t* rowp = base + h * 16 * ROWB;
+				if(WIDE) *reinterpret_cast<uint2*>(rowp) = make_uint2(v[0], v[V - 1]);
+				else *reinterpret_cast<uint32_t*>(rowp) = v[0];
+#pragma unroll
+				for(int n = 1; n < 16; n++) {
+					const int gray = n ^ (n >> 1);
+					const int bit = (n & 1) ? 0 : (n & 2) ? 1 : (n & 4) ? 2 : 3;
+#pragma unroll
+					for(int c = 0; c < V; c++) v[c] ^= x[bit][c];
+					if(WIDE) *reinterpret_cast<uint2*>(rowp + gray * ROWB) = make_uint2(v[0], v[V - 1]);
+					else *reinterpret_cast<uint32_t*>(rowp + gray * ROWB) = v[0];
+				}
+			}
+			for(int j = bt; j < RT; j += 128) {
+				unsigned r = rbase + j;
+				idxs[b * RT + j] = r < R ? __ldg(idx + (size_t)r * G + g) : make_uint4(0, 0, 0, 0);
+			}
+			mbar_arrive(&bars[b]);  // release: this thread's table rows and index bytes
+		}
+		return;
+	}
+
+	// ---------------- lookups
+	uint32_t acc[RPW][16][V];
+#pragma unroll
+	for(int s = 0; s < RPW; s++)
+#pragma unroll
+		for(int k = 0; k < 16; k++)
+#pragma unroll
+			for(int c = 0; c < V; c++) acc[s][k][c] = 0;
+	const uint32_t lwb = (uint32_t)lane * 4 * V;
+
+	auto lookups = [&](int b) {
+		const uint32_t lw = lwb + b * (ROWB / 2);
+#pragma unroll
+		for(int s = 0; s < RPW; s++) {
+			const int j = warp * RPW + s;
+			if(rbase + j < R) {
+				const uint4 q = idxs[b * RT + j];
+				const uint32_t qq[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+				for(int k = 0; k < 16; k++) {
+					uint32_t addr;
+					if(WIDE) {
+						// (m << 9) | lw: byte1 <- m << 1 is not a byte move, so build m << 8 and double it
+						const uint32_t sel = 4u | ((uint32_t)(k & 3) << 4) | (5u << 8) | (5u << 12);
+						addr = (__byte_perm(qq[k >> 2], 0, sel & 0xFFF0u | 5u) << 1) | lw;
+					} else {
+						const uint32_t sel = 4u | ((uint32_t)(k & 3) << 4) | (5u << 8) | (5u << 12);
+						addr = __byte_perm(qq[k >> 2], lw, sel);
+					}
+					if(WIDE) {
+						uint2 t;
+						if(ASMLD) asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(t.x), "=r"(t.y) : "r"(sbase + addr));
+						else t = *reinterpret_cast<const uint2*>(tbl + addr);
+						acc[s][k][0] ^= t.x;
+						acc[s][k][V - 1] ^= t.y;
+					} else {
+						uint32_t t;
+						if(ASMLD) asm volatile("ld.shared.u32 %0, [%1];" : "=r"(t) : "r"(sbase + addr));
+						else t = *reinterpret_cast<const uint32_t*>(tbl + addr);
+						acc[s][k][0] ^= t;
+					}
+				}
+			}
+		}
+	};
+	bool ok = true;
+	for(unsigned g = 0; g < G && ok; g += 2) {
+		if(!mbar_wait(&bars[0], (g >> 1) & 1)) { ok = false; break; }
+		lookups(0);
+		__syncwarp();
+		if(lane == 0) mbar_arrive(&bars[2]);
+		if(g + 1 >= G) break;
+		if(!mbar_wait(&bars[1], (g >> 1) & 1)) { ok = false; break; }
+		lookups(1);
+		__syncwarp();
+		if(lane == 0) mbar_arrive(&bars[3]);
+	}
+	if(!ok) return;
+
+#pragma unroll
+	for(int s = 0; s < RPW; s++) {
+		const unsigned r = rbase + warp * RPW + s;
+		if(r < R && laneIn) {
+#pragma unroll
+			for(int c = 0; c < V; c++) {
+				uint32_t v = acc[s][15][c];
+#pragma unroll
+				for(int k = 14; k >= 0; k--) v = mul2x2(v) ^ acc[s][k][c];
+				uint32_t* p = reinterpret_cast<uint32_t*>(rec + (size_t)r * recPitch + colWord) + c;
+				if(accumulate) v ^= *p;
+				*p = v;
+			}
+		}
+	}
+}
+
+template<int RPW, int NL, int WIDE, bool ASMLD>
+static int launch_comb_ws(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec,
+                          size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st)
+{
+	constexpr int RT = RPW * NL;
+	constexpr int V = WIDE ? 2 : 1;
+	const size_t smem = 65536 * V + 2 * RT * sizeof(uint4) + 4 * sizeof(uint64_t);
+	P2C_CUDA_TRY(cudaFuncSetAttribute(k_comb_ws<RPW, NL, WIDE, ASMLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const unsigned G = (nIn + 7) / 8;
+	const size_t TW = P2C_TILE_WORDS * V;
+	dim3 grid((unsigned)((nWords + TW - 1) / TW), (R + RT - 1) / RT);
+	k_comb_ws<RPW, NL, WIDE, ASMLD><<<grid, (NL + 4) * 32, smem, st>>>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate,
+	                                                                 round_up(nWords, P2C_TILE_WORDS));
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
+int comb_error_take() {
+	unsigned v = 0, z = 0;
+	if(cudaMemcpyFromSymbol(&v, g_comb_error, sizeof(v)) != cudaSuccess) return -1;
+	if(v) cudaMemcpyToSymbol(g_comb_error, &z, sizeof(z));
+	return (int)v;
+}
+
 static std::atomic<int> g_comb_shape{0};
 int set_comb_shape(int shape) { return g_comb_shape.exchange(shape); }
+
+// Automatic CTA shape from R.  Per recovery row the large shapes run at the
+// same rate (measured: 96-row blocks of the one-phase kernel and 72- or 60-row
+// blocks of the warp-specialised kernel), so for R > 64 the shape with the
+// fewest padded rows in the last block wins; small R uses narrow CTAs.
+int comb_auto_shape(unsigned R) {
+	if(R <= 8) return 1;        // 1 warp x 8 rows
+	if(R <= 32) return 2;       // 4 warps x 8 rows
+	if(R <= 64) return 3;       // 8 warps x 8 rows
+	static const int cand[3][2] = {{4, 96}, {11, 72}, {12, 60}};
+	int best = 4;
+	unsigned bestRows = ~0u;
+	for(const auto& c : cand) {
+		unsigned rows = (R + c[1] - 1) / c[1] * c[1];
+		if(rows < bestRows) { bestRows = rows; best = c[0]; }
+	}
+	return best;
+}
 
 // Chooses the CTA shape from R: full 96-row blocks for large R, fewer warps /
 // rows per warp for small R so that little of a block is wasted.
@@ -223,12 +460,7 @@ int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* i
 		return 0;
 	}
 	if(shape <= 0) shape = g_comb_shape.load();
-	if(shape <= 0) {
-		if(R <= 8) shape = 1;        // 1 warp x 8 rows
-		else if(R <= 32) shape = 2;  // 4 warps x 8 rows
-		else if(R <= 64) shape = 3;  // 8 warps x 8 rows
-		else shape = 4;              // 12 warps x 8 rows
-	}
+	if(shape <= 0) shape = comb_auto_shape(R);
 	switch(shape) {
 	case 1: return launch_comb<8, 1>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 2: return launch_comb<8, 4>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
@@ -238,6 +470,12 @@ int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* i
 	case 7: return launch_comb<5, 16>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 8: return launch_comb<4, 16>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 9: return launch_comb<2, 32>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 10: return launch_comb_ws<8, 8, 0, false>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 11: return launch_comb_ws<6, 12, 0, false>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 12: return launch_comb_ws<5, 12, 0, false>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 13: return launch_comb_ws<6, 12, 0, true>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 14: return launch_comb_ws<3, 12, 1, false>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 15: return launch_comb_ws<4, 8, 1, false>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	default: return launch_comb<8, 12>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	}
 }
@@ -246,7 +484,7 @@ int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* i
 unsigned long long comb_units(unsigned R, size_t nWords, int shape) {
 	static const int rt[10] = {96, 8, 32, 64, 96, 80, 84, 80, 64, 64};
 	if(shape <= 0) shape = g_comb_shape.load();
-	if(shape <= 0) shape = R <= 8 ? 1 : R <= 32 ? 2 : R <= 64 ? 3 : 4;
+	if(shape <= 0) shape = comb_auto_shape(R);
 	const unsigned RT = rt[shape > 9 ? 0 : shape];
 	return (unsigned long long)((nWords + P2C_TILE_WORDS - 1) / P2C_TILE_WORDS) * ((R + RT - 1) / RT);
 }

@@ -45,6 +45,10 @@ int comb_batched(const BatchJob* dJobs, unsigned nJobs, unsigned long long total
 
 // process-wide CTA shape override for the comb kernel (0 = choose from R); returns the previous value
 int set_comb_shape(int shape);
+// shape chosen for R when none is set
+int comb_auto_shape(unsigned R);
+// reads and clears the device error flag of the comb kernels (1 = a bounded wait timed out)
+int comb_error_take();
 
 // bit-sliced LOP3 kernel and split-nibble table kernel (same contract, coefficient matrix [R][nIn])
 int xor_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,

@@ -269,7 +269,7 @@ def test_large_shapes_sampled(n, R, S):
     _sampled_check(torch, d_in, pw, n, d_rec, R, S, exps)
 
 
-@pytest.mark.parametrize("shape", list(range(0, 10)))
+@pytest.mark.parametrize("shape", list(range(0, 16)))
 def test_comb_every_cta_shape(shape):
     """Every comb CTA shape (rows per warp x warps) gives the oracle's result,
     including partial recovery blocks and a ragged input group."""
@@ -290,6 +290,7 @@ def test_comb_every_cta_shape(shape):
                                      1, scratch.data_ptr(), sb, None), "muladd")
         torch.cuda.synchronize()
         got = d_rec.cpu().numpy().view(np.uint8)[:, :S]
+        assert L.par2cuda_device_error() == 0
         assert np.array_equal(got, O.recover_coeffs(host_in, np.full(n, S), coeff))
     finally:
         L.par2cuda_set_comb_shape(prev)
