@@ -222,7 +222,7 @@ def run_ours(args, cfg, file_lens):
 
     S, N, R = cfg["S"], cfg["N"], cfg["R"]
     mul_adds = N * R * (S // 2)
-    job = ResidentJob(S, file_lens, list(range(R)), device=local)
+    job = ResidentJob(S, file_lens, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
     job.fill_synthetic(seed=1 + rank)
     torch.cuda.synchronize()
 
@@ -352,6 +352,7 @@ def run_ours(args, cfg, file_lens):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "src_GBps_x_recovery": N * S * R * world / (ms / 1e3) / 1e9,
         "kernels_ms": {"comb_muladd": comb_ms, "file_md5": hash_ms, "step": ms},
+        "method": args.method,
         "roofline": {"bound": "int-alu", "kernel": "k_comb_muladd", "achieved": 2 * comb_rate / 1e12,
                      "peak": alu_peak, "unit": "Tops/s", "frac": 2 * comb_rate / 1e12 / alu_peak,
                      "traffic": None, "alg_bytes": alg_bytes,
@@ -477,6 +478,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--cpu-window", type=int, default=32768)
+    ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor"], default="comb",
+                    help="multiply-accumulate kernel of the resident-job workloads")
     ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline.traffic")

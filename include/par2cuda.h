@@ -53,7 +53,8 @@ enum {
 	PAR2CUDA_METHOD_AUTO = 0,
 	PAR2CUDA_METHOD_COMB = 1,   /* shared-memory XOR-combination tables (default) */
 	PAR2CUDA_METHOD_XOR = 2,    /* LOP3, per-coefficient-bit masks */
-	PAR2CUDA_METHOD_NIBBLE = 3  /* shared-memory split-nibble tables */
+	PAR2CUDA_METHOD_NIBBLE = 3, /* shared-memory split-nibble tables */
+	PAR2CUDA_METHOD_TENSOR = 4  /* tcgen05 GF(2) bit-matrix product (e4m3 0/1, fp32 accumulators) */
 };
 
 typedef struct par2cuda_info {

@@ -15,8 +15,9 @@ DONE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int)
 PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint)
 
 ADD_OK, ADD_OK_BUSY, ADD_FULL = 0, 1, 2
-METHOD_AUTO, METHOD_COMB, METHOD_XOR, METHOD_NIBBLE = 0, 1, 2, 3
-METHOD_NAMES = {"auto": METHOD_AUTO, "comb": METHOD_COMB, "xor": METHOD_XOR, "nibble": METHOD_NIBBLE}
+METHOD_AUTO, METHOD_COMB, METHOD_XOR, METHOD_NIBBLE, METHOD_TENSOR = 0, 1, 2, 3, 4
+METHOD_NAMES = {"auto": METHOD_AUTO, "comb": METHOD_COMB, "xor": METHOD_XOR, "nibble": METHOD_NIBBLE,
+                "tensor": METHOD_TENSOR}
 
 
 class Info(ctypes.Structure):

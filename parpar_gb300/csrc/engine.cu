@@ -158,7 +158,8 @@ int Engine::alloc_processing() {
 		P2C_CUDA_TRY(cudaHostAlloc(&hFlags, R ? R : 1, cudaHostAllocDefault));
 	}
 	// scratch: index bytes + coefficient matrix + checksum accumulators + flags
-	size_t need = round_up(idx_bytes((unsigned)R, batchPad), 256) + round_up(R * batchPad * 2, 256) +
+	size_t need = round_up(std::max(idx_bytes((unsigned)R, batchPad), tc_scratch_bytes((unsigned)R, batchPad)), 256) +
+	              round_up(R * batchPad * 2, 256) +
 	              round_up(std::max<size_t>(R, batchPad) * 8, 256) + round_up(R, 256);
 	if(need > scratchBytes) {
 		if(dScratch) cudaFree(dScratch);
@@ -173,7 +174,7 @@ int Engine::alloc_processing() {
 int Engine::init(int m, unsigned inputBatch) {
 	if(!sliceSize) { set_error("setSliceSize must be called before init"); return -1; }
 	method = m == 0 ? 1 : m;
-	if(method < 1 || method > 3) { set_error("unknown method %d", m); return -1; }
+	if(method < 1 || method > 4) { set_error("unknown method %d", m); return -1; }
 	inputBatchSize = inputBatch ? inputBatch : (unsigned)default_batch(sliceSize);
 	if(inputBatchSize > 32768) { set_error("input batch size %u > 32768", inputBatchSize); return -1; }
 	batchPad = (unsigned)round_up(inputBatchSize, 8);
@@ -527,7 +528,7 @@ int Engine::run_kernel(unsigned areaIdx, unsigned numInputs) {
 	// scratch carve-up
 	uint8_t* sp = reinterpret_cast<uint8_t*>(dScratch);
 	uint4* dIdx = reinterpret_cast<uint4*>(sp);
-	sp += round_up(idx_bytes(R, batchPad), 256);
+	sp += round_up(std::max(idx_bytes(R, batchPad), tc_scratch_bytes(R, batchPad)), 256);
 	uint16_t* dCoeff = reinterpret_cast<uint16_t*>(sp);
 	sp += round_up((size_t)R * batchPad * 2, 256);
 	unsigned long long* dCk = reinterpret_cast<unsigned long long*>(sp);
@@ -540,6 +541,8 @@ int Engine::run_kernel(unsigned areaIdx, unsigned numInputs) {
 	int rc = 0;
 	if(method == 2) rc = xor_muladd(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, sCompute);
 	else if(method == 3) rc = nibble_muladd_t(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, gt, sCompute);
+	else if(method == 4) rc = tc_muladd(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, true, dIdx,
+	                                    tc_scratch_bytes(R, numInputs), sCompute);
 	else rc = comb_muladd(a.dIn, pitch, numInputs, dIdx, dRec, recPitchAlloc, R, nWords, acc, shape, sCompute);
 	if(rc) return -1;
 	processingAdd = true;
@@ -565,7 +568,7 @@ int Engine::do_end(const Req& r) {
 	const unsigned R = (unsigned)outputExponents.size();
 	if(processingAdd && R) {
 		uint8_t* sp = reinterpret_cast<uint8_t*>(dScratch);
-		sp += round_up(idx_bytes(R, batchPad), 256);
+		sp += round_up(std::max(idx_bytes(R, batchPad), tc_scratch_bytes(R, batchPad)), 256);
 		sp += round_up((size_t)R * batchPad * 2, 256);
 		unsigned long long* dCk = reinterpret_cast<unsigned long long*>(sp);
 		sp += round_up(std::max<size_t>(R, batchPad) * 8, 256);
@@ -617,8 +620,9 @@ int Engine::info(par2cuda_info* o) {
 	o->device = device;
 	cudaDeviceProp p;
 	if(cudaGetDeviceProperties(&p, device) == cudaSuccess) snprintf(o->device_name, sizeof(o->device_name), "%.127s", p.name);
-	const char* names[] = {"auto", "Comb (XOR-combination tables)", "Xor (LOP3 bit masks)", "Nibble tables"};
-	snprintf(o->method_desc, sizeof(o->method_desc), "%s", names[method >= 0 && method <= 3 ? method : 0]);
+	const char* names[] = {"auto", "Comb (XOR-combination tables)", "Xor (LOP3 bit masks)", "Nibble tables",
+	                       "Tensor (tcgen05 GF(2) bit-matrix, e4m3)"};
+	snprintf(o->method_desc, sizeof(o->method_desc), "%s", names[method >= 0 && method <= 4 ? method : 0]);
 	o->staging_count = (unsigned)staging.size();
 	o->staging_size = inputBatchSize;
 	o->min_staging_size = minInBatchSize;

@@ -66,6 +66,12 @@ int file_md5(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_
 int rows_md5(const void* rows, size_t pitchBytes, unsigned n, size_t dataLen, const uint8_t* dPrefix, unsigned prefixLen,
              uint8_t* dOut, cudaStream_t st);
 
+// tensor-core (tcgen05, e4m3 0/1 operands, fp32 accumulators) variant, coefficient matrix [R][nIn]
+int tc_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec, size_t recPitch,
+              unsigned R, size_t nWords, int accumulate, bool fp8, void* scratch, size_t scratchBytes, cudaStream_t st);
+size_t tc_scratch_bytes(unsigned R, unsigned nIn);
+int tc_error_take();
+
 // seeded synthetic bytes (parpar_gb300/synth.py layout); byteOffset (a
 // multiple of 8) selects a window of each row's byte stream
 int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first, cudaStream_t st,

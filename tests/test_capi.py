@@ -40,7 +40,7 @@ def test_host_helpers_without_gpu():
     # pitch: data padded to 8 bytes + 8-byte checksum, rounded to 128 bytes
     for s, p in [(2, 128), (120, 128), (121, 256), (1 << 20, (1 << 20) + 128)]:
         assert lib.par2cuda_row_pitch_bytes(s) == p
-    assert lib.par2cuda_muladd_scratch_bytes(10, 100) == (10 * 13 * 16 + 255) // 256 * 256
+    assert lib.par2cuda_muladd_scratch_bytes(10, 100) == (max(10 * 13 * 16, 10 * 100 * 32) + 255) // 256 * 256
 
 
 def test_create_fails_cleanly_without_device():

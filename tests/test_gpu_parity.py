@@ -19,7 +19,7 @@ from parpar_gb300.gfproc import GfProc, GfProcError, create_recovery
 
 pytestmark = pytest.mark.gpu
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
-METHODS = ["comb", "xor", "nibble"]
+METHODS = ["comb", "xor", "nibble", "tensor"]
 
 
 def golden_inputs(c):
@@ -171,7 +171,7 @@ def _dev_rows(torch, n, S, seed, first=0):
     return t, pitch // 2
 
 
-@pytest.mark.parametrize("method", [0, 1, 2, 3])
+@pytest.mark.parametrize("method", [0, 1, 2, 3, 4])
 def test_device_muladd_accumulate(method):
     torch = pytest.importorskip("torch")
     L = _lib.load()
@@ -195,6 +195,28 @@ def test_device_muladd_accumulate(method):
     _lib.check(L.par2cuda_muladd(d_in[half:].data_ptr(), pw, n - half, c2.data_ptr(), d_rec.data_ptr(), pw, R,
                                  nw, 1, method, scratch.data_ptr(), sb, None), "muladd")
     torch.cuda.synchronize()
+    assert L.par2cuda_device_error() == 0
+    got = d_rec.cpu().numpy().view(np.uint8)[:, :S]
+    assert np.array_equal(got, O.recover_coeffs(host_in, np.full(n, S), coeff))
+
+
+@pytest.mark.parametrize("n,R,S", [(1, 1, 2), (8, 16, 512), (100, 40, 3000), (257, 17, 4100)])
+def test_tensor_core_variant(n, R, S):
+    """The tcgen05 variant: pipeline wrap (more stages than the 3-stage ring),
+    partial recovery blocks and word tiles, one input, many inputs."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    d_in, pw = _dev_rows(torch, n, S, 77 + n)
+    host_in = synth.slices(77 + n, 0, n, S)
+    coeff = np.random.default_rng(n).integers(0, 65536, size=(R, n), dtype=np.uint16)
+    d_coeff = torch.from_numpy(coeff.view(np.int16)).cuda()
+    d_rec = torch.zeros((R, pw), dtype=torch.int16, device="cuda")
+    sb = L.par2cuda_muladd_scratch_bytes(R, n)
+    scratch = torch.zeros(sb, dtype=torch.uint8, device="cuda")
+    _lib.check(L.par2cuda_muladd(d_in.data_ptr(), pw, n, d_coeff.data_ptr(), d_rec.data_ptr(), pw, R, S // 2, 0,
+                                 _lib.METHOD_TENSOR, scratch.data_ptr(), sb, None), "muladd")
+    torch.cuda.synchronize()
+    assert L.par2cuda_device_error() == 0
     got = d_rec.cpu().numpy().view(np.uint8)[:, :S]
     assert np.array_equal(got, O.recover_coeffs(host_in, np.full(n, S), coeff))
 
