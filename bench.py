@@ -17,6 +17,7 @@ reference algorithm's CPU implementation on this host's cores.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -324,6 +325,58 @@ def run_ours(args, cfg, file_lens):
         e2e = {"value": mul_adds * world / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": N * S,
                "d2h_bytes_per_step": job.d2h_bytes(), "ms_per_step": ems,
                "path": "par2cuda C ABI: pinned host slices -> H2D -> job -> D2H recovery + IFSC + file MD5 + verdicts"}
+    # e2e through the reference-facing plugin boundary: the PAR2ProcCUDA engine
+    # driven like GfProc (src/gf.cc AddSlice / EndInput / GetOutputSlice) with
+    # pinned host slices; GF + internal checksum only (the reference's plugin
+    # does not hash; hashing is HasherInput's job)
+    e2e_plugin = None
+    if not args.no_e2e and not args.no_plugin:
+        from parpar_gb300.gfproc import GfProc
+        from parpar_gb300.job import file_layout
+        _, row_lens = file_layout(file_lens, S)
+        g = GfProc(S, method=args.method)
+        g.set_recovery_slices(list(range(R)))
+        views = [host_in[i, : int(row_lens[i])] for i in range(N)]
+
+        L2 = _lib.load()
+        ctx = g._ctx
+        ptrs = [v.data_ptr() for v in views]
+        lens_ = [int(x) for x in row_lens]
+        verdict = (ctypes.c_int * R)()
+        null_cb = _lib.DONE_FN()  # NULL: no completion callback
+
+        @_lib.DONE_FN
+        def on_out(user, status):
+            verdict[user or 0] = status
+
+        def plugin_pass():
+            # the calls a native adapter makes: discardOutput, waitForAdd +
+            # addInput per slice, endInput, getOutput per recovery slice
+            L2.par2cuda_discard_output(ctx)
+            for i in range(N):
+                L2.par2cuda_wait_for_add(ctx)
+                _lib.check(L2.par2cuda_add_input(ctx, ptrs[i], lens_[i], i, 0, null_cb, None), "add")
+            _lib.check(L2.par2cuda_end_input(ctx, null_cb, None), "end")
+            _lib.check(L2.par2cuda_sync(ctx), "sync")
+            for r in range(R):
+                _lib.check(L2.par2cuda_get_output(ctx, r, rec_host[r].data_ptr(), on_out, r), "get")
+            _lib.check(L2.par2cuda_sync(ctx), "sync")
+            return all(verdict[r] == 1 for r in range(R))
+        plugin_pass()
+        t0p = time.perf_counter()
+        okp = True
+        for _ in range(args.plugin_steps):
+            okp = plugin_pass() and okp
+        tp = (time.perf_counter() - t0p) / args.plugin_steps
+        assert okp, "plugin path checksum verdict failed"
+        inf = g.info()
+        g.close()
+        e2e_plugin = {"value": mul_adds * world / tp, "unit": UNIT, "h2d_bytes_per_step": int(row_lens.sum()),
+                      "d2h_bytes_per_step": R * S, "ms_per_step": tp * 1e3, "steps": args.plugin_steps,
+                      "batch": inf["staging_size"], "staging_areas": inf["staging_count"], "method_desc": inf["method_desc"],
+                      "path": "C ABI plugin calls from the host: wait_for_add + add_input x N (pinned host slices), "
+                              "end_input, get_output x R (verdict callbacks); GF multiply-accumulate + internal "
+                              "checksum, no hashing (the reference plugin does not hash); host wall clock"}
     stop.set()
     if th:
         th.join(timeout=3)
@@ -364,6 +417,7 @@ def run_ours(args, cfg, file_lens):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "e2e": e2e,
+        "e2e_plugin": e2e_plugin,
     }
     if args.traffic_bytes:
         line["roofline"]["traffic"] = args.traffic_bytes
@@ -477,6 +531,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
+    ap.add_argument("--no-plugin", action="store_true", help="skip the plugin-boundary e2e measurement")
+    ap.add_argument("--plugin-steps", type=int, default=2)
     ap.add_argument("--cpu-window", type=int, default=32768)
     ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor"], default="comb",
                     help="multiply-accumulate kernel of the resident-job workloads")

@@ -584,34 +584,39 @@ int Engine::do_end(const Req& r) {
 
 int Engine::do_output(const Req& r) {
 	const size_t S = currentSliceSize;
-	int valid = 1;
 	if(!processingAdd) {
 		memset(const_cast<void*>(r.buf), 0, S); // nothing computed -> zeros (controller.cpp:376-382)
-	} else {
-		// ordered after the end-of-input verification on the compute stream
-		cudaEvent_t ev = take_event();
-		P2C_CUDA_TRY(cudaEventRecord(ev, sCompute));
-		P2C_CUDA_TRY(cudaStreamWaitEvent(sOut, ev, 0));
-		give_event(ev);
-		const uint16_t* src = dRec + (size_t)r.slot * recPitchAlloc;
-		void* out = const_cast<void*>(r.buf);
-		if(is_pinned(out)) {
-			P2C_CUDA_TRY(cudaMemcpyAsync(out, src, S, cudaMemcpyDefault, sOut));
-			P2C_CUDA_TRY(cudaStreamSynchronize(sOut));
-		} else {
-			if(hOutBounceBytes < S) {
-				if(hOutBounce) cudaFreeHost(hOutBounce);
-				hOutBounce = nullptr;
-				P2C_CUDA_TRY(cudaHostAlloc(&hOutBounce, S, cudaHostAllocDefault));
-				hOutBounceBytes = S;
-			}
-			P2C_CUDA_TRY(cudaMemcpyAsync(hOutBounce, src, S, cudaMemcpyDeviceToHost, sOut));
-			P2C_CUDA_TRY(cudaStreamSynchronize(sOut));
-			memcpy(out, hOutBounce, S);
-		}
-		valid = hFlags ? hFlags[r.slot] : 0;
+		if(r.cb) r.cb(r.user, 1);
+		return 0;
 	}
-	if(r.cb) r.cb(r.user, valid);
+	// ordered after the end-of-input verification on the compute stream
+	cudaEvent_t ev = take_event();
+	P2C_CUDA_TRY(cudaEventRecord(ev, sCompute));
+	P2C_CUDA_TRY(cudaStreamWaitEvent(sOut, ev, 0));
+	give_event(ev);
+	const uint16_t* src = dRec + (size_t)r.slot * recPitchAlloc;
+	void* out = const_cast<void*>(r.buf);
+	const unsigned slot = r.slot;
+	par2cuda_done_fn cb = r.cb;
+	void* user = r.user;
+	if(is_pinned(out)) {
+		// asynchronous: the verdict callback fires from the notifier thread once
+		// the copy (and the verification it is ordered after) has completed
+		P2C_CUDA_TRY(cudaMemcpyAsync(out, src, S, cudaMemcpyDefault, sOut));
+		notify_after(sOut, [this, slot, cb, user] { if(cb) cb(user, hFlags ? hFlags[slot] : 0); });
+		return 0;
+	}
+	if(hOutBounceBytes < S) {
+		P2C_CUDA_TRY(cudaStreamSynchronize(sOut));
+		if(hOutBounce) cudaFreeHost(hOutBounce);
+		hOutBounce = nullptr;
+		P2C_CUDA_TRY(cudaHostAlloc(&hOutBounce, S, cudaHostAllocDefault));
+		hOutBounceBytes = S;
+	}
+	P2C_CUDA_TRY(cudaMemcpyAsync(hOutBounce, src, S, cudaMemcpyDeviceToHost, sOut));
+	P2C_CUDA_TRY(cudaStreamSynchronize(sOut));
+	memcpy(out, hOutBounce, S);
+	if(cb) cb(user, hFlags ? hFlags[slot] : 0);
 	return 0;
 }
 
