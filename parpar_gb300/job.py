@@ -173,5 +173,43 @@ class ResidentJob:
             flags = self.d_flags.to("cpu", non_blocking=True)
         return rec_host, ifsc, fmd5, flags
 
+    # -------------------------------------------------------------- PAR2 packets
+    def md5_16k(self) -> list:
+        """MD5 of the first 16 KiB of every file (the FileDesc / file ID hash),
+        on the device: one thread per file over its first row(s)."""
+        L = self.L
+        out = [None] * len(self.file_lens)
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        groups = {}
+        for f, ln in enumerate(self.file_lens):
+            groups.setdefault(min(16384, ln), []).append(f)
+        for n, files in groups.items():
+            if n > self.S:
+                # the first 16 KiB span several rows: hash them as one stream
+                flen = torch.tensor([n] * len(files), dtype=torch.int64, device=self.dev)
+                first = torch.tensor([int(self.first_row[f]) for f in files], dtype=torch.int32, device=self.dev)
+                d = torch.empty(16 * len(files), dtype=torch.uint8, device=self.dev)
+                _lib.check(L.par2cuda_file_md5(self.d_in.data_ptr(), self.pitch, len(files), flen.data_ptr(),
+                                              first.data_ptr(), self.S, d.data_ptr(), st), "md5_16k")
+            else:
+                rows = self.d_in[torch.tensor([int(self.first_row[f]) for f in files], device=self.dev)].contiguous()
+                d = torch.empty(16 * len(files), dtype=torch.uint8, device=self.dev)
+                _lib.check(L.par2cuda_rows_md5(rows.data_ptr(), self.pitch, len(files), n, None, 0, d.data_ptr(), st),
+                           "md5_16k")
+            h = d.cpu().numpy().reshape(len(files), 16)
+            for k, f in enumerate(files):
+                out[f] = h[k].tobytes()
+        return out
+
+    def recovery_packet_md5s(self, set_id: bytes):
+        """Packet MD5 of every recovery slice packet (MD5 over set ID, type,
+        exponent and the slice), one GPU thread per recovery row."""
+        from .par2packets import recovery_prefixes
+        pre = torch.from_numpy(np.ascontiguousarray(recovery_prefixes(set_id, self.exps))).to(self.dev)
+        d = torch.empty(16 * self.R, dtype=torch.uint8, device=self.dev)
+        _lib.check(self.L.par2cuda_rows_md5(self.d_rec.data_ptr(), self.pitch, self.R, self.S, pre.data_ptr(), 36,
+                                           d.data_ptr(), torch.cuda.current_stream(self.dev).cuda_stream), "rows_md5")
+        return [bytes(x) for x in d.cpu().numpy().reshape(self.R, 16)]
+
     def d2h_bytes(self):
         return self.R * self.S + self.N * 20 + len(self.file_lens) * 16 + self.R
