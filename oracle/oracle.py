@@ -28,7 +28,8 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
         os.makedirs(BUILD_DIR, exist_ok=True)
         tmp = LIB + ".tmp.%d" % os.getpid()
-        subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-pthread", "-std=gnu99",
+        isa = ["-march=armv8-a+crc"] if os.uname().machine == "aarch64" else []
+        subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-pthread", "-std=gnu11", *isa,
                                "-fno-strict-aliasing", "-o", tmp, SRC])
         os.replace(tmp, LIB)
     return LIB
@@ -54,6 +55,10 @@ def lib():
         L.or_md5.restype = None; L.or_md5.argtypes = [vp, sz, ctypes.c_uint64, vp]
         L.or_crc32.restype = ctypes.c_uint32; L.or_crc32.argtypes = [vp, sz, ctypes.c_uint64]
         L.or_hash_file.restype = None; L.or_hash_file.argtypes = [vp, sz, sz, vp, vp]
+        L.or_recover_fast.restype = i32
+        L.or_recover_fast.argtypes = [vp, ctypes.c_uint, sz, vp, ctypes.c_uint, vp, i32]
+        L.or_fast_method.restype = ctypes.c_char_p
+        L.or_crc32_fast.restype = ctypes.c_uint32; L.or_crc32_fast.argtypes = [vp, sz, ctypes.c_uint64]
         L.or_hash_rows.restype = None
         L.or_hash_rows.argtypes = [vp, sz, sz, vp, ctypes.c_uint, vp, vp, i32]
         _lib = L
@@ -120,6 +125,18 @@ def recover_coeffs(inputs: np.ndarray, lens, coeffs_rn: np.ndarray, threads: int
     rc = lib().or_recover_coeffs(_p(inputs), _p(lens), _p(c), n, S, r, _p(out), threads)
     if rc:
         raise RuntimeError("oracle recover failed: %d" % rc)
+    return out
+
+
+def recover_fast(inputs: np.ndarray, coeffs_rn: np.ndarray, threads: int = 1) -> np.ndarray:
+    """Baseline-speed CPU recovery of zero-padded rows (see or_recover_fast)."""
+    inputs = np.ascontiguousarray(inputs, dtype=np.uint8)
+    n, S = inputs.shape
+    c = np.ascontiguousarray(coeffs_rn, dtype=np.uint16)
+    out = np.zeros((c.shape[0], S), dtype=np.uint8)
+    rc = lib().or_recover_fast(_p(inputs), n, S, _p(c), c.shape[0], _p(out), threads)
+    if rc:
+        raise RuntimeError("oracle recover_fast failed: %d" % rc)
     return out
 
 

@@ -349,6 +349,8 @@ void or_hash_file(const uint8_t* data, size_t len, size_t sliceSize, uint8_t* if
 	or_md5(data, len, 0, fileMd5);
 }
 
+uint32_t or_crc32_fast(const uint8_t* data, size_t len, uint64_t zeroPad);
+
 /* ---------- MD5 of many equal-length buffers (threaded; hashing baseline) ---------- */
 typedef struct { const uint8_t* base; size_t stride, len; const size_t* lens; uint64_t pad; unsigned n, nt, tid; uint8_t* md5; uint32_t* crc; } or_hjob;
 static void* or_hworker(void* arg) {
@@ -357,7 +359,7 @@ static void* or_hworker(void* arg) {
 		size_t l = j->lens ? j->lens[i] : j->len;
 		uint64_t pad = j->lens ? (uint64_t)(j->len - l) : j->pad;
 		or_md5(j->base + (size_t)i * j->stride, l, pad, j->md5 + 16 * (size_t)i);
-		if(j->crc) j->crc[i] = or_crc32(j->base + (size_t)i * j->stride, l, pad);
+		if(j->crc) j->crc[i] = or_crc32_fast(j->base + (size_t)i * j->stride, l, pad);
 	}
 	return NULL;
 }
@@ -377,3 +379,150 @@ void or_hash_rows(const uint8_t* base, size_t stride, size_t len, const size_t* 
 	for(int t = 0; t < threads; t++) pthread_create(&th[t], NULL, or_hworker, &jobs[t]);
 	for(int t = 0; t < threads; t++) pthread_join(th[t], NULL);
 }
+
+/* ---------- CPU baseline: the reference's fastest method on this host ----------
+ * or_recover_fast computes the same product as or_recover for zero-padded
+ * input rows (lens = slice).  On aarch64 it restates the reference's NEON
+ * split-nibble SHUFFLE method (gf16/gf16_shuffle_neon.c): per coefficient,
+ * eight 16-byte tables (4 nibble positions x low/high result byte), 16 words
+ * per step de-interleaved into low/high bytes with vld2q_u8, eight TBL
+ * lookups per recovery row, accumulators for two recovery rows held in L1 and
+ * re-interleaved with vst2q_u8.  Elsewhere it falls back to or_recover.
+ * Used only as the timed CPU baseline; the tests check it against or_recover. */
+#if defined(__aarch64__) && defined(__ARM_NEON)
+#include <arm_neon.h>
+#define OR_FAST_NEON 1
+#define OR_CHUNK_WORDS 4096
+
+typedef struct {
+	const uint8_t* inputs; const uint16_t* coeffs; unsigned n, r; size_t slice; uint8_t* out;
+	unsigned nthreads, tid;
+} or_fjob;
+
+static void or_nib_tables(uint16_t c, uint8x16_t tl[4], uint8x16_t th[4]) {
+	uint8_t lo[4][16], hi[4][16];
+	for(int q = 0; q < 4; q++)
+		for(int v = 0; v < 16; v++) {
+			uint16_t p = or_mul(c, (uint16_t)(v << (4 * q)));
+			lo[q][v] = (uint8_t)p;
+			hi[q][v] = (uint8_t)(p >> 8);
+		}
+	for(int q = 0; q < 4; q++) { tl[q] = vld1q_u8(lo[q]); th[q] = vld1q_u8(hi[q]); }
+}
+
+static void* or_fast_worker(void* arg) {
+	or_fjob* j = (or_fjob*)arg;
+	const size_t words = j->slice / 2;
+	const size_t vecWords = words / 16 * 16;          /* NEON part; tail done with lookups */
+	const unsigned nchunks = (unsigned)((vecWords + OR_CHUNK_WORDS - 1) / OR_CHUNK_WORDS);
+	const unsigned pairs = (j->r + 1) / 2;
+	uint8_t* acc = (uint8_t*)aligned_alloc(64, 4 * OR_CHUNK_WORDS); /* [row 0 lo|hi][row 1 lo|hi] */
+	const size_t units = (size_t)nchunks * pairs;
+	for(size_t u = j->tid; u < units; u += j->nthreads) {
+		const unsigned ch = (unsigned)(u / pairs), pr = (unsigned)(u % pairs);
+		const size_t w0 = (size_t)ch * OR_CHUNK_WORDS;
+		const size_t nw = vecWords - w0 < OR_CHUNK_WORDS ? vecWords - w0 : OR_CHUNK_WORDS;
+		const unsigned r0 = pr * 2, nr = (r0 + 1 < j->r) ? 2 : 1;
+		memset(acc, 0, 4 * OR_CHUNK_WORDS);
+		for(unsigned i = 0; i < j->n; i++) {
+			uint8x16_t tl[2][4], th[2][4];
+			for(unsigned o = 0; o < nr; o++) or_nib_tables(j->coeffs[(size_t)(r0 + o) * j->n + i], tl[o], th[o]);
+			if(nr == 1) for(int q = 0; q < 4; q++) { tl[1][q] = vdupq_n_u8(0); th[1][q] = vdupq_n_u8(0); }
+			const uint8_t* src = j->inputs + (size_t)i * j->slice + 2 * w0;
+			const uint8x16_t m4 = vdupq_n_u8(15);
+			for(size_t b = 0; b < nw / 16; b++) {
+				uint8x16x2_t v = vld2q_u8(src + 32 * b);
+				uint8x16_t n0 = vandq_u8(v.val[0], m4), n1 = vshrq_n_u8(v.val[0], 4);
+				uint8x16_t n2 = vandq_u8(v.val[1], m4), n3 = vshrq_n_u8(v.val[1], 4);
+				for(int o = 0; o < 2; o++) {
+					uint8x16_t rl = veorq_u8(veorq_u8(vqtbl1q_u8(tl[o][0], n0), vqtbl1q_u8(tl[o][1], n1)),
+					                         veorq_u8(vqtbl1q_u8(tl[o][2], n2), vqtbl1q_u8(tl[o][3], n3)));
+					uint8x16_t rh = veorq_u8(veorq_u8(vqtbl1q_u8(th[o][0], n0), vqtbl1q_u8(th[o][1], n1)),
+					                         veorq_u8(vqtbl1q_u8(th[o][2], n2), vqtbl1q_u8(th[o][3], n3)));
+					uint8_t* al = acc + o * 2 * OR_CHUNK_WORDS + 16 * b;
+					uint8_t* ah = al + OR_CHUNK_WORDS;
+					vst1q_u8(al, veorq_u8(vld1q_u8(al), rl));
+					vst1q_u8(ah, veorq_u8(vld1q_u8(ah), rh));
+				}
+			}
+		}
+		for(unsigned o = 0; o < nr; o++) {
+			uint8_t* dst = j->out + (size_t)(r0 + o) * j->slice + 2 * w0;
+			const uint8_t* al = acc + o * 2 * OR_CHUNK_WORDS;
+			for(size_t b = 0; b < nw / 16; b++) {
+				uint8x16x2_t z;
+				z.val[0] = vld1q_u8(al + 16 * b);
+				z.val[1] = vld1q_u8(al + OR_CHUNK_WORDS + 16 * b);
+				vst2q_u8(dst + 32 * b, z);
+			}
+		}
+	}
+	free(acc);
+	return NULL;
+}
+#endif
+
+int or_recover_fast(const uint8_t* inputs, unsigned n, size_t slice, const uint16_t* coeffs, unsigned r,
+                    uint8_t* out, int threads) {
+	or_init();
+	if(slice & 1) return -1;
+	if(threads < 1) threads = 1;
+	if(threads > 256) threads = 256;
+#ifdef OR_FAST_NEON
+	const size_t words = slice / 2, vecWords = words / 16 * 16;
+	pthread_t th[256];
+	or_fjob jobs[256];
+	for(int t = 0; t < threads; t++) {
+		or_fjob jb = {inputs, coeffs, n, r, slice, out, (unsigned)threads, (unsigned)t};
+		jobs[t] = jb;
+	}
+	for(int t = 0; t < threads; t++) pthread_create(&th[t], NULL, or_fast_worker, &jobs[t]);
+	for(int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+	if(vecWords < words) { /* tail words with the table method */
+		for(unsigned row = 0; row < r; row++) {
+			uint8_t* dst = out + (size_t)row * slice + 2 * vecWords;
+			memset(dst, 0, 2 * (words - vecWords));
+			for(unsigned i = 0; i < n; i++)
+				or_muladd_region(dst, inputs + (size_t)i * slice + 2 * vecWords, words - vecWords, coeffs[(size_t)row * n + i]);
+		}
+	}
+	return 0;
+#else
+	size_t* lens = (size_t*)malloc(sizeof(size_t) * (n ? n : 1));
+	if(!lens) return -2;
+	for(unsigned i = 0; i < n; i++) lens[i] = slice;
+	int rc = or_recover_coeffs(inputs, lens, coeffs, n, slice, r, out, threads);
+	free(lens);
+	return rc;
+#endif
+}
+
+const char* or_fast_method(void) {
+#ifdef OR_FAST_NEON
+	return "NEON split-nibble shuffle (restating the reference's SHUFFLE_NEON method)";
+#else
+	return "portable LOOKUP (the reference's portable method)";
+#endif
+}
+
+/* CRC32 for the baseline's hashing: the ARMv8 CRC32 instructions where the
+ * host has them (the reference's ARMCRC hasher), else the table method. */
+#if defined(__aarch64__) && defined(__ARM_FEATURE_CRC32)
+#include <arm_acle.h>
+uint32_t or_crc32_fast(const uint8_t* data, size_t len, uint64_t zeroPad) {
+	uint32_t c = 0xFFFFFFFFu;
+	size_t i = 0;
+	for(; i + 8 <= len; i += 8) { uint64_t v; memcpy(&v, data + i, 8); c = __crc32d(c, v); }
+	for(; i < len; i++) c = __crc32b(c, data[i]);
+	/* zero padding by x^(8n) as in or_crc32 */
+	uint32_t xn = 0x00800000u;
+	while(zeroPad) {
+		if(zeroPad & 1) c = or_crc_mulmod(c, xn);
+		xn = or_crc_mulmod(xn, xn);
+		zeroPad >>= 1;
+	}
+	return ~c;
+}
+#else
+uint32_t or_crc32_fast(const uint8_t* data, size_t len, uint64_t zeroPad) { return or_crc32(data, len, zeroPad); }
+#endif

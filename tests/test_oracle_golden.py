@@ -94,3 +94,17 @@ def test_md5multi(case):
     bufs = synth.slices(case["seed"], 0, case["n"], case["len"])
     md5s, _ = O.hash_rows(bufs)
     assert md5s.tobytes().hex() == case["md5"]
+
+
+def test_fast_baseline_path_matches_oracle():
+    """The CPU baseline's fast path (NEON on aarch64, the plain method
+    elsewhere) computes the same recovery and CRCs as the oracle."""
+    rng = np.random.default_rng(8)
+    for n, r, S in [(5, 3, 64), (17, 5, 8192 + 34), (3, 1, 32), (9, 4, 2)]:
+        x = rng.integers(0, 256, size=(n, S), dtype=np.uint8)
+        c = rng.integers(0, 65536, size=(r, n), dtype=np.uint16)
+        assert np.array_equal(O.recover_fast(x, c, threads=3), O.recover_coeffs(x, np.full(n, S), c))
+    L = O.lib()
+    for ln, pad in [(0, 5), (13, 0), (1000, 77), (64, 4096)]:
+        d = rng.integers(0, 256, size=ln, dtype=np.uint8)
+        assert L.or_crc32_fast(O._p(d), ln, pad) == O.crc32(d, pad)
