@@ -159,8 +159,18 @@ uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent);
 /* CTA shape of the comb kernel for every later call in this process (the
  * autotuner's knob): 0 = chosen from the number of recovery rows, 1..9 = a
  * fixed (rows per warp x warps) shape; 10..15 = warp-specialised shapes
- * (4 table-building warps + 8 or 12 lookup warps, 2 or 4 words per lane).  Returns the previous setting. */
+ * (4 table-building warps + 8 or 12 lookup warps, 2 or 4 words per lane);
+ * 16..22 = warp-specialised shapes with two 8-input tables per ring slot
+ * (20: one table, same prefetching builders).  Returns the previous setting. */
 int par2cuda_set_comb_shape(int shape);
+/* The comb CTA shape the next multiply-accumulate with num_rec recovery rows
+ * will use (the set_comb_shape setting, else the automatic choice). */
+int par2cuda_comb_shape_for(unsigned num_rec);
+/* Measures the current device's three-input LOP3 throughput (ops/s) with a
+ * calibration kernel at full occupancy (about 0.1 s): the denominator of the
+ * integer-ALU roofline (2 LOP3 per word multiply-accumulate).  No counterpart
+ * in the reference. */
+int par2cuda_lop3_rate(double* ops_per_s, void* stream);
 /* Reads and clears the device-side error flag of the multiply-accumulate
  * kernels: 1 when a bounded wait inside a kernel gave up (its results are then
  * invalid), 0 otherwise, negative if the flag could not be read. */
@@ -246,8 +256,9 @@ int par2cuda_coeff_index(const uint16_t* d_coeff, unsigned num_rec, unsigned num
  * (set_coeffs, gf16/controller_cpu.cpp:372-379, without a host matrix). */
 int par2cuda_par2_index(const uint16_t* d_input_nums, unsigned num_in, const uint16_t* d_exponents, unsigned num_rec,
                         void* d_index, void* stream);
-/* Work units of a job with num_rec rows of n_words words for CTA shape 1..4
- * (8 x {1,4,8,12} recovery rows per unit). */
+/* Work units of a job with num_rec rows of n_words words for batched CTA
+ * shape 1..7 (1..4: one-phase, 8 x {1,4,8,12} recovery rows per unit; 5..7:
+ * paired tables, {72,64,32} rows per unit); 0 for an unknown shape. */
 unsigned long long par2cuda_batch_units(unsigned num_rec, size_t n_words, int shape);
 /* One persistent launch over d_jobs[0..num_jobs) (device array). */
 int par2cuda_batch_muladd(const par2cuda_batch_job* d_jobs, unsigned num_jobs, unsigned long long total_units,

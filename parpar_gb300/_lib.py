@@ -20,6 +20,15 @@ METHOD_NAMES = {"auto": METHOD_AUTO, "comb": METHOD_COMB, "xor": METHOD_XOR, "ni
                 "tensor": METHOD_TENSOR}
 
 
+def comb_kernel_name(shape: int) -> str:
+    """Kernel behind a comb CTA shape id (par2cuda_set_comb_shape)."""
+    if 10 <= shape <= 15:
+        return "k_comb_ws"
+    if shape >= 16:
+        return "k_comb_pair"
+    return "k_comb_muladd"
+
+
 class Info(ctypes.Structure):
     _fields_ = [
         ("device", ctypes.c_int),
@@ -70,6 +79,8 @@ SIGNATURES = [
     ("par2cuda_coeff", _u16, [_u16, _u16]),
     ("par2cuda_set_comb_shape", _i, [_i]),
     ("par2cuda_device_error", _i, []),
+    ("par2cuda_lop3_rate", _i, [ctypes.POINTER(ctypes.c_double), _vp]),
+    ("par2cuda_comb_shape_for", _i, [_u]),
     ("par2cuda_muladd_scratch_bytes", _sz, [_u, _u]),
     ("par2cuda_muladd", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _i, _vp, _sz, _vp]),
     ("par2cuda_muladd_noalloc", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _vp]),

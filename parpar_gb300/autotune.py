@@ -14,8 +14,11 @@ import torch
 
 from . import _lib
 
-# shape id -> recovery rows per CTA (8 rows per warp x warps)
-SHAPES = {1: 8, 2: 32, 3: 64, 4: 96}
+# batched shape id -> recovery rows per CTA: 1..4 one-phase tables (8 rows
+# per warp x 1, 4, 8, 12 warps), 5..7 paired tables with table-building warps
+SHAPES = {1: 8, 2: 32, 3: 64, 4: 96, 5: 72, 6: 64, 7: 32}
+# the single-job kernel with the same CTA configuration (timed in its place)
+SINGLE = {1: 1, 2: 2, 3: 3, 4: 4, 5: 16, 6: 18, 7: 23}
 BUCKETS = [8, 16, 32, 64, 96, 128, 192, 100000]
 
 _cache: dict = {}
@@ -39,7 +42,7 @@ def _time_shape(shape: int, R: int, n: int = 256, slice_bytes: int = 262144, rep
     sb = L.par2cuda_muladd_scratch_bytes(R, n)
     scratch = torch.empty(max(sb, 256), dtype=torch.uint8, device="cuda")
     nw = ((slice_bytes + 7) // 8 * 8 + 8) // 2
-    prev = L.par2cuda_set_comb_shape(shape)
+    prev = L.par2cuda_set_comb_shape(SINGLE[shape])
     try:
         def once():
             _lib.check(L.par2cuda_muladd(d_in.data_ptr(), pw, n, coeff.data_ptr(), d_rec.data_ptr(), pw, R, nw, 0,
@@ -61,7 +64,7 @@ def _time_shape(shape: int, R: int, n: int = 256, slice_bytes: int = 262144, rep
 
 
 def best_shape(R: int) -> int:
-    """Fastest batched comb shape (1..4) for R recovery rows on this device."""
+    """Fastest batched comb shape (1..7) for R recovery rows on this device."""
     dev = torch.cuda.current_device()
     key = (dev, _bucket(R))
     if key not in _cache:

@@ -125,8 +125,15 @@ uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent) {
 }
 
 int par2cuda_set_comb_shape(int shape) {
-	if(shape < 0 || shape > 15) { p2c::set_error("comb shape %d out of range 0..15", shape); return -1; }
+	if(shape < 0 || shape > 25) { p2c::set_error("comb shape %d out of range 0..25", shape); return -1; }
 	return p2c::set_comb_shape(shape);
+}
+
+int par2cuda_comb_shape_for(unsigned num_rec) { return p2c::comb_shape_for(num_rec); }
+
+int par2cuda_lop3_rate(double* ops_per_s, void* stream) {
+	if(!ops_per_s) { p2c::set_error("lop3_rate: null output"); return -1; }
+	return p2c::lop3_rate(ops_per_s, (cudaStream_t)stream);
 }
 
 int par2cuda_device_error(void) {
@@ -215,7 +222,6 @@ int par2cuda_par2_index(const uint16_t* d_input_nums, unsigned num_in, const uin
 }
 
 unsigned long long par2cuda_batch_units(unsigned num_rec, size_t n_words, int shape) {
-	if(shape < 1 || shape > 4) return 0;
 	return p2c::comb_units(num_rec, n_words, shape);
 }
 

@@ -421,6 +421,267 @@ static int launch_comb_ws(const uint16_t* in, size_t inPitch, unsigned nIn, cons
 	return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Paired-table form: each ring slot holds GP tables (GP consecutive 8-input
+// groups, table t at +t*64 KiB, so both reads of a (row, k) pair share the
+// PRMT-built address form and differ in the LDS immediate).  With GP = 2 the
+// two lookups of a (row, k) pair fold into one three-input XOR
+//     P[r][k] ^= T_2s[ idx[r][2s][k] ] ^ T_2s+1[ idx[r][2s+1][k] ]
+// so a lookup costs one LDS, one PRMT and half a LOP3 (the one-table forms
+// spend a full LOP3 per lookup; the ALU pipe runs at half the LSU rate in
+// warp instructions, so the XOR count matters as much as the LDS count).
+// Builders prefetch the next slot's inputs and index rows into registers
+// before waiting for the slot's buffer to drain.  Waits are bounded as in
+// k_comb_ws.
+// One work unit (word tile x RT recovery rows, all inputs) of the paired
+// form.  Slots are numbered globally from gs0 so that a persistent CTA keeps
+// its mbarrier phases running from unit to unit.  Returns false when a
+// bounded wait gave up (g_comb_error is set); the thread then does no more
+// work in this unit but still returns normally.
+template<int RPW, int NL, int GP>
+__device__ __forceinline__ bool pair_unit(
+	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
+	const uint4* __restrict__ idx, unsigned G,
+	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate,
+	size_t tile, unsigned rbase, unsigned gs0, uint8_t* smem)
+{
+	static_assert(GP == 1 || GP == 2, "one or two tables per slot");
+	constexpr int RT = RPW * NL;
+	constexpr int TBL = 65536;                         // 256 rows x 256 B (two ring buffers interleaved)
+	constexpr int NJ = (RT * GP + 127) / 128;          // index rows staged per builder thread
+	uint8_t* tbl = smem;
+	uint4* idxs = reinterpret_cast<uint4*>(smem + GP * TBL);                  // [2][GP][RT]
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + GP * TBL + 2 * GP * RT * sizeof(uint4)); // full[2], empty[2]
+
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const size_t colWord = tile * P2C_TILE_WORDS + lane * 2;
+	const unsigned NS = (G + GP - 1) / GP;             // ring slots of this unit
+
+	if(warp >= NL) {
+		// ---------------- builders: 4 warps x 4 high nibbles of each table
+		const int bw = warp - NL;
+		const int bt = threadIdx.x - NL * 32; // 0..127
+		uint32_t x[GP][8];
+		uint4 ip[NJ];
+		auto fetch = [&](unsigned s) {
+#pragma unroll
+			for(int t = 0; t < GP; t++)
+#pragma unroll
+				for(int u = 0; u < 8; u++) {
+					const unsigned i = (s * GP + t) * 8 + u;
+					x[t][u] = i < nIn ? __ldg(reinterpret_cast<const uint32_t*>(in + (size_t)i * inPitch + colWord)) : 0u;
+				}
+#pragma unroll
+			for(int q = 0; q < NJ; q++) {
+				const int jj = bt + q * 128;           // jj = t * RT + j
+				ip[q] = make_uint4(0, 0, 0, 0);
+				if(jj < GP * RT) {
+					const int t = jj / RT, j = jj - t * RT;
+					const unsigned g = s * GP + t, r = rbase + j;
+					if(g < G && r < R) ip[q] = __ldg(idx + (size_t)r * G + g);
+				}
+			}
+		};
+		if(NS) fetch(0);
+		for(unsigned s = 0; s < NS; s++) {
+			const unsigned gs = gs0 + s;
+			const int b = gs & 1;
+			if(gs >= 2 && !mbar_wait(&bars[2 + b], ((gs >> 1) - 1) & 1)) return false;
+#pragma unroll
+			for(int t = 0; t < GP; t++) {
+				uint8_t* base = tbl + t * TBL + b * 128 + lane * 4;
+#pragma unroll
+				for(int hh = 0; hh < 4; hh++) {
+					const int h = bw * 4 + hh;
+					uint32_t v = 0;
+#pragma unroll
+					for(int u = 0; u < 4; u++) if(h >> u & 1) v ^= x[t][4 + u];
+					uint8_t* rowp = base + h * 16 * 256;
+					*reinterpret_cast<uint32_t*>(rowp) = v;
+#pragma unroll
+					for(int n = 1; n < 16; n++) {
+						const int gray = n ^ (n >> 1);
+						const int bit = (n & 1) ? 0 : (n & 2) ? 1 : (n & 4) ? 2 : 3;
+						v ^= x[t][bit];
+						*reinterpret_cast<uint32_t*>(rowp + gray * 256) = v;
+					}
+				}
+			}
+#pragma unroll
+			for(int q = 0; q < NJ; q++) {
+				const int jj = bt + q * 128;
+				if(jj < GP * RT) idxs[b * GP * RT + jj] = ip[q];
+			}
+			mbar_arrive(&bars[b]);  // release: this thread's table rows and index rows
+			if(s + 1 < NS) fetch(s + 1);
+		}
+		return true;
+	}
+
+	// ---------------- lookups
+	uint32_t acc[RPW][16];
+#pragma unroll
+	for(int s = 0; s < RPW; s++)
+#pragma unroll
+		for(int k = 0; k < 16; k++) acc[s][k] = 0;
+	const uint32_t lwb = (uint32_t)lane * 4;
+
+	for(unsigned sl = 0; sl < NS; sl++) {
+		const unsigned gs = gs0 + sl;
+		const int b = gs & 1;
+		if(!mbar_wait(&bars[b], (gs >> 1) & 1)) return false;
+		const uint32_t lw = lwb + b * 128;
+#pragma unroll
+		for(int s = 0; s < RPW; s++) {
+			const int j = warp * RPW + s;
+			if(rbase + j < R) {
+				uint32_t qq[GP][4];
+#pragma unroll
+				for(int t = 0; t < GP; t++) {
+					const uint4 q = idxs[(b * GP + t) * RT + j];
+					qq[t][0] = q.x; qq[t][1] = q.y; qq[t][2] = q.z; qq[t][3] = q.w;
+				}
+#pragma unroll
+				for(int k = 0; k < 16; k++) {
+					// byte0 <- lw.byte0, byte1 <- q.byte(k&3), bytes 2,3 <- lw.byte1 (= 0)
+					const uint32_t sel = 4u | ((uint32_t)(k & 3) << 4) | (5u << 8) | (5u << 12);
+					uint32_t v = *reinterpret_cast<const uint32_t*>(tbl + __byte_perm(qq[0][k >> 2], lw, sel));
+					if(GP == 2) v ^= *reinterpret_cast<const uint32_t*>(tbl + TBL + __byte_perm(qq[GP - 1][k >> 2], lw, sel));
+					acc[s][k] ^= v;
+				}
+			}
+		}
+		__syncwarp();
+		if(lane == 0) mbar_arrive(&bars[2 + b]);
+	}
+
+#pragma unroll
+	for(int s = 0; s < RPW; s++) {
+		const unsigned r = rbase + warp * RPW + s;
+		if(r < R) {
+			uint32_t v = acc[s][15];
+#pragma unroll
+			for(int k = 14; k >= 0; k--) v = mul2x2(v) ^ acc[s][k];
+			uint32_t* p = reinterpret_cast<uint32_t*>(rec + (size_t)r * recPitch + colWord);
+			if(accumulate) v ^= *p;
+			*p = v;
+		}
+	}
+	return true;
+}
+
+template<int RPW, int NL, int GP>
+__device__ __forceinline__ void pair_init_bars(uint8_t* smem) {
+	constexpr int RT = RPW * NL;
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + GP * 65536 + 2 * GP * RT * sizeof(uint4));
+	if(threadIdx.x == 0) {
+		mbar_init(&bars[0], 128);
+		mbar_init(&bars[1], 128);
+		mbar_init(&bars[2], NL);
+		mbar_init(&bars[3], NL);
+	}
+}
+
+template<int RPW, int NL, int GP>
+__global__ void __launch_bounds__((NL + 4) * 32, 1) k_comb_pair(
+	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
+	const uint4* __restrict__ idx, unsigned G,
+	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate)
+{
+	extern __shared__ __align__(16) uint8_t smem[];
+	pair_init_bars<RPW, NL, GP>(smem);
+	__syncthreads();
+	// one-dimensional grid, recovery blocks fastest: the CTAs that read the
+	// same input tile run at the same time and share it through L2
+	const unsigned rblocks = (R + RPW * NL - 1) / (RPW * NL);
+	const size_t tile = blockIdx.x / rblocks;
+	const unsigned rb = blockIdx.x - (unsigned)tile * rblocks;
+	pair_unit<RPW, NL, GP>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate, tile, rb * (RPW * NL), 0u, smem);
+}
+
+// Persistent batched form of the paired kernel: as k_comb_batched, one CTA
+// per SM takes (job, word tile, recovery block) units from an atomic ticket.
+// The mbarrier ring runs on across units (global slot numbering); a
+// __syncthreads separates units, and a unit whose bounded wait gave up stops
+// the CTA for good (every thread leaves the loop at the same barrier).
+template<int RPW, int NL, int GP>
+__global__ void __launch_bounds__((NL + 4) * 32, 1) k_comb_pair_batched(
+	const BatchJob* __restrict__ jobs, unsigned nJobs, unsigned long long totalUnits,
+	unsigned long long* __restrict__ counter)
+{
+	constexpr int RT = RPW * NL;
+	extern __shared__ __align__(16) uint8_t smem[];
+	__shared__ unsigned long long s_unit;
+	__shared__ unsigned s_job;
+	__shared__ int s_abort;
+	pair_init_bars<RPW, NL, GP>(smem);
+	if(threadIdx.x == 0) s_abort = 0;
+	__syncthreads();
+	unsigned gs = 0;
+	for(;;) {
+		if(threadIdx.x == 0) {
+			unsigned long long u = atomicAdd(counter, 1ull);
+			s_unit = u;
+			unsigned lo = 0, hi = nJobs;
+			while(hi - lo > 1) {
+				unsigned mid = (lo + hi) >> 1;
+				if(jobs[mid].unitBase <= u) lo = mid; else hi = mid;
+			}
+			s_job = lo;
+		}
+		__syncthreads();
+		const unsigned long long u = s_unit;
+		if(u >= totalUnits || s_abort) break;
+		const BatchJob& J = jobs[s_job];
+		const unsigned long long local = u - J.unitBase;
+		const unsigned rblocks = (J.R + RT - 1) / RT;
+		const size_t tile = (size_t)(local / rblocks);
+		const unsigned rb = (unsigned)(local % rblocks);
+		const unsigned G = (J.nIn + 7) / 8;
+		if(!pair_unit<RPW, NL, GP>(J.in, J.inPitch, J.nIn, J.idx, G, J.rec, J.recPitch, J.R, J.accumulate,
+		                           tile, rb * RT, gs, smem))
+			s_abort = 1;
+		gs += (G + GP - 1) / GP;
+		__syncthreads(); // s_unit / s_job are rewritten next round
+	}
+}
+
+template<int RPW, int NL, int GP>
+static int launch_comb_pair(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec,
+                            size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st)
+{
+	constexpr int RT = RPW * NL;
+	const size_t smem = 65536 * GP + 2 * GP * RT * sizeof(uint4) + 4 * sizeof(uint64_t);
+	P2C_CUDA_TRY(cudaFuncSetAttribute(k_comb_pair<RPW, NL, GP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const unsigned G = (nIn + 7) / 8;
+	const unsigned long long ctas = (unsigned long long)((nWords + P2C_TILE_WORDS - 1) / P2C_TILE_WORDS) * ((R + RT - 1) / RT);
+	if(ctas > 0x7FFFFFFFull) { set_error("comb: %llu CTAs exceed the grid limit", ctas); return -1; }
+	k_comb_pair<RPW, NL, GP><<<(unsigned)ctas, (NL + 4) * 32, smem, st>>>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate);
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
+template<int RPW, int NL, int GP>
+static int launch_pair_batched(const BatchJob* jobs, unsigned nJobs, unsigned long long totalUnits,
+                               unsigned long long* counter, cudaStream_t st)
+{
+	constexpr int RT = RPW * NL;
+	const size_t smem = 65536 * GP + 2 * GP * RT * sizeof(uint4) + 4 * sizeof(uint64_t);
+	P2C_CUDA_TRY(cudaFuncSetAttribute(k_comb_pair_batched<RPW, NL, GP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	int dev = 0, sms = 0;
+	P2C_CUDA_TRY(cudaGetDevice(&dev));
+	P2C_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	int occ = 1;
+	P2C_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_comb_pair_batched<RPW, NL, GP>, (NL + 4) * 32, smem));
+	if(occ < 1) occ = 1;
+	unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)sms * occ, totalUnits);
+	if(!grid) return 0;
+	P2C_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+	k_comb_pair_batched<RPW, NL, GP><<<grid, (NL + 4) * 32, smem, st>>>(jobs, nJobs, totalUnits, counter);
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
 int comb_error_take() {
 	unsigned v = 0, z = 0;
 	if(cudaMemcpyFromSymbol(&v, g_comb_error, sizeof(v)) != cudaSuccess) return -1;
@@ -431,22 +692,21 @@ int comb_error_take() {
 static std::atomic<int> g_comb_shape{0};
 int set_comb_shape(int shape) { return g_comb_shape.exchange(shape); }
 
-// Automatic CTA shape from R.  Per recovery row the large shapes run at the
-// same rate (measured: 96-row blocks of the one-phase kernel and 72- or 60-row
-// blocks of the warp-specialised kernel), so for R > 64 the shape with the
-// fewest padded rows in the last block wins; small R uses narrow CTAs.
+// Automatic CTA shape from R (measured on 2000 x 1 MiB and 4096 x 256 KiB
+// jobs): above 8 rows the paired-table kernel wins even with padded rows
+// (R = 16: 2.1 T vs 1.8 T word mul-adds/s for the best narrow shape), with
+// 72-row blocks (6 rows x 12 lookup warps) or 64-row blocks (8 x 8, 3 %
+// slower per row), whichever costs less after padding the last block.  Up to
+// 8 rows a single-warp one-phase CTA builds its own tables.
 int comb_auto_shape(unsigned R) {
-	if(R <= 8) return 1;        // 1 warp x 8 rows
-	if(R <= 32) return 2;       // 4 warps x 8 rows
-	if(R <= 64) return 3;       // 8 warps x 8 rows
-	static const int cand[3][2] = {{4, 96}, {11, 72}, {12, 60}};
-	int best = 4;
-	unsigned bestRows = ~0u;
-	for(const auto& c : cand) {
-		unsigned rows = (R + c[1] - 1) / c[1] * c[1];
-		if(rows < bestRows) { bestRows = rows; best = c[0]; }
-	}
-	return best;
+	if(R <= 8) return 1;
+	const unsigned r72 = (R + 71) / 72 * 72, r64 = (R + 63) / 64 * 64;
+	return (double)r72 <= (double)r64 / 0.97 ? 16 : 18;
+}
+
+int comb_shape_for(unsigned R) {
+	const int s = g_comb_shape.load();
+	return s > 0 ? s : comb_auto_shape(R);
 }
 
 // Chooses the CTA shape from R: full 96-row blocks for large R, fewer warps /
@@ -476,16 +736,31 @@ int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* i
 	case 13: return launch_comb_ws<6, 12, 0, true>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 14: return launch_comb_ws<3, 12, 1, false>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 15: return launch_comb_ws<4, 8, 1, false>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 16: return launch_comb_pair<6, 12, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 17: return launch_comb_pair<5, 12, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 18: return launch_comb_pair<8, 8, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 19: return launch_comb_pair<7, 10, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 20: return launch_comb_pair<6, 12, 1>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 21: return launch_comb_pair<4, 16, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 22: return launch_comb_pair<3, 20, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 23: return launch_comb_pair<8, 4, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 24: return launch_comb_pair<8, 2, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 25: return launch_comb_pair<8, 1, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	default: return launch_comb<8, 12>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	}
 }
 
-// units per job for a shape: word tiles x recovery blocks
+// recovery rows per CTA of the persistent batched shapes: 1..4 one-phase
+// (8 rows per warp x 1, 4, 8, 12 warps), 5..7 paired (72, 64, 32 rows)
+int batched_rows(int shape) {
+	static const int rt[8] = {0, 8, 32, 64, 96, 72, 64, 32};
+	return shape >= 1 && shape <= 7 ? rt[shape] : 0;
+}
+
+// units per job for a batched shape: word tiles x recovery blocks
 unsigned long long comb_units(unsigned R, size_t nWords, int shape) {
-	static const int rt[10] = {96, 8, 32, 64, 96, 80, 84, 80, 64, 64};
-	if(shape <= 0) shape = g_comb_shape.load();
-	if(shape <= 0) shape = comb_auto_shape(R);
-	const unsigned RT = rt[shape > 9 ? 0 : shape];
+	const unsigned RT = (unsigned)batched_rows(shape);
+	if(!RT) return 0;
 	return (unsigned long long)((nWords + P2C_TILE_WORDS - 1) / P2C_TILE_WORDS) * ((R + RT - 1) / RT);
 }
 
@@ -520,7 +795,10 @@ int comb_batched(const BatchJob* dJobs, unsigned nJobs, unsigned long long total
 	case 2: return launch_batched<8, 4>(dJobs, nJobs, totalUnits, dCounter, 0, st);
 	case 3: return launch_batched<8, 8>(dJobs, nJobs, totalUnits, dCounter, 0, st);
 	case 4: return launch_batched<8, 12>(dJobs, nJobs, totalUnits, dCounter, 0, st);
-	default: set_error("batched comb shape %d not available (1..4)", shape); return -1;
+	case 5: return launch_pair_batched<6, 12, 2>(dJobs, nJobs, totalUnits, dCounter, st);
+	case 6: return launch_pair_batched<8, 8, 2>(dJobs, nJobs, totalUnits, dCounter, st);
+	case 7: return launch_pair_batched<8, 4, 2>(dJobs, nJobs, totalUnits, dCounter, st);
+	default: set_error("batched comb shape %d not available (1..7)", shape); return -1;
 	}
 }
 

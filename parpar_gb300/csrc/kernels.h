@@ -47,8 +47,11 @@ int comb_batched(const BatchJob* dJobs, unsigned nJobs, unsigned long long total
 int set_comb_shape(int shape);
 // shape chosen for R when none is set
 int comb_auto_shape(unsigned R);
+int comb_shape_for(unsigned R);  // the shape the next comb call with R rows uses
 // reads and clears the device error flag of the comb kernels (1 = a bounded wait timed out)
 int comb_error_take();
+// measured three-input LOP3 throughput of the current device (ops/s)
+int lop3_rate(double* opsPerSec, cudaStream_t st);
 
 // bit-sliced LOP3 kernel and split-nibble table kernel (same contract, coefficient matrix [R][nIn])
 int xor_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,

@@ -19,7 +19,7 @@ def oracle_rec(spec):
     return O.recover(x, np.full(spec.N, spec.S), np.arange(spec.N), spec.exps)
 
 
-@pytest.mark.parametrize("fixed_shape", [None, 1, 2, 3, 4])
+@pytest.mark.parametrize("fixed_shape", [None, 1, 2, 3, 4, 5, 6, 7])
 def test_batched_passes_match_oracle(fixed_shape):
     torch = pytest.importorskip("torch")
     from parpar_gb300.batch import BatchRunner

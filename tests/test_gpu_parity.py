@@ -291,7 +291,7 @@ def test_large_shapes_sampled(n, R, S):
     _sampled_check(torch, d_in, pw, n, d_rec, R, S, exps)
 
 
-@pytest.mark.parametrize("shape", list(range(0, 16)))
+@pytest.mark.parametrize("shape", list(range(0, 26)))
 def test_comb_every_cta_shape(shape):
     """Every comb CTA shape (rows per warp x warps) gives the oracle's result,
     including partial recovery blocks and a ragged input group."""
@@ -316,3 +316,16 @@ def test_comb_every_cta_shape(shape):
         assert np.array_equal(got, O.recover_coeffs(host_in, np.full(n, S), coeff))
     finally:
         L.par2cuda_set_comb_shape(prev)
+
+
+def test_lop3_rate_calibration():
+    """The integer-ALU roofline denominator: a positive, plausible LOP3 rate
+    (between 32 and 256 lanes per SM per clock at 1-2.2 GHz)."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    L = _lib.load()
+    v = ctypes.c_double(0)
+    _lib.check(L.par2cuda_lop3_rate(ctypes.byref(v), None), "lop3_rate")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    per_sm_clk = v.value / sms / 2.0e9
+    assert 16 < per_sm_clk < 300, v.value
