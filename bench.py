@@ -498,6 +498,7 @@ def run_batched_workload(args, cfg):
     lat = runner.run_per_job()
     t_job = time.perf_counter() - t0
     assert runner.all_valid()
+    mode_ms = runner.tune_mode()   # persistent launch vs per-job grid launches, pass 0 timed on the device
     runner.capture()
     for _ in range(args.warmup):
         runner.run_batched()
@@ -531,6 +532,7 @@ def run_batched_workload(args, cfg):
         "per_job_launch": {"jobs_per_s": len(jobs) / t_job, "s": t_job,
                            "p50_job_s": float(np.percentile(lat, 50)), "p99_job_s": float(np.percentile(lat, 99))},
         "speedup_vs_per_job_launch": (len(jobs) / (ms / 1e3)) / (len(jobs) / t_job),
+        "batched_mode": runner.mode, "mode_pass0_ms": mode_ms,
         "autotune": {str(k): v[0] for k, v in autotune.table().items()},
         "gpu_launches": runner.launches_per_run() * args.steps,
         "clocks": summarize_clocks(clock_lines, 0),

@@ -14,9 +14,15 @@ Two ways to run a mix:
     device-level C-ABI calls (synthetic window, zero pad + checksum, comb
     multiply-accumulate, verification), then wait for the job;
   * batched (`capture` + `run_batched`): per pass the window kernels of all
-    jobs and one persistent comb launch per CTA-shape group (jobs grouped by
-    the autotuner's shape for their recovery count), all captured once into a
-    CUDA graph and replayed.
+    jobs, then the multiply-accumulate of all jobs, then their verification,
+    captured once into a CUDA graph and replayed.  The multiply-accumulate
+    runs in one of two modes, chosen by timing one pass of each
+    (`tune_mode`):
+      - "persistent": one persistent comb launch per CTA-shape group (jobs
+        grouped by the autotuner's shape for their recovery count), CTAs
+        taking (job, tile, recovery block) units from an atomic ticket;
+      - "grid": each job's own grid launch of its automatic shape, the jobs
+        spread over four side streams so that small jobs overlap.
 """
 from __future__ import annotations
 
@@ -99,7 +105,12 @@ class _JobBufs:
 
 
 class BatchRunner:
-    def __init__(self, jobs, budget_bytes: int = 64 << 30, device: int = 0, shape_of=None):
+    MODES = ("persistent", "grid")
+
+    def __init__(self, jobs, budget_bytes: int = 64 << 30, device: int = 0, shape_of=None, mode: str = "persistent"):
+        if mode not in self.MODES:
+            raise ValueError("mode must be one of %s" % (self.MODES,))
+        self.mode = mode
         self.L = _lib.load()
         self.dev = torch.device("cuda", device)
         # largest jobs first: their units are handed out first, the tail is small units
@@ -138,6 +149,13 @@ class BatchRunner:
     def _n_words(n_bytes: int) -> int:
         return ((n_bytes + 7) // 8 * 8 + 8) // 2
 
+    def _muladd_grid(self, b: _JobBufs, p: int, st):
+        """One job's window through the single-job C-ABI call (grid launch)."""
+        off, n = b.window(p)
+        _lib.check(self.L.par2cuda_muladd(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_coeff.data_ptr(), b.d_rec.data_ptr(),
+                                          b.pw, b.spec.R, self._n_words(n), 0, _lib.METHOD_COMB, b.d_idx.data_ptr(),
+                                          b.d_idx.numel(), st), "muladd")
+
     # ------------------------------------------------------------ per-job path
     def run_per_job(self, verify_cb=None):
         """Each job on its own: its launches for every pass, then wait for it.
@@ -153,11 +171,7 @@ class BatchRunner:
             for p in range(self.P):
                 if not self._window_prep(b, p, st):
                     continue
-                off, n = b.window(p)
-                sb = L.par2cuda_muladd_scratch_bytes(b.spec.R, b.spec.N)
-                _lib.check(L.par2cuda_muladd(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_coeff.data_ptr(), b.d_rec.data_ptr(),
-                                             b.pw, b.spec.R, self._n_words(n), 0, _lib.METHOD_COMB, b.d_idx.data_ptr(),
-                                             b.d_idx.numel(), st), "muladd")
+                self._muladd_grid(b, p, st)
                 self._verify(b, p, st)
                 if verify_cb:
                     verify_cb(b, p)
@@ -205,22 +219,64 @@ class BatchRunner:
             live = [ji for ji, b in enumerate(self.bufs) if b.window(p)[1] > 0]
             for ji in live:
                 self._window_prep(self.bufs[ji], p, st)
-            # one persistent launch per shape group, groups concurrently on side streams
-            for gi, (shape, members) in enumerate(sorted(groups.items())):
-                members = [ji for ji in members if ji in live]
-                if not members:
-                    continue
-                d, total, counter, shp = self._pass_descs(p, members)
-                side = self._side[gi % len(self._side)]
+            for side in self._side:
                 side.wait_stream(cur)
-                _lib.check(self.L.par2cuda_batch_muladd(d.data_ptr(), len(members), total, counter.data_ptr(), shp,
-                                                        side.cuda_stream), "batch_muladd")
-            for gi in range(len(groups)):
-                cur.wait_stream(self._side[gi % len(self._side)])
+            if self.mode == "persistent":
+                # one persistent launch per shape group, groups concurrently on side streams
+                for gi, (shape, members) in enumerate(sorted(groups.items())):
+                    members = [ji for ji in members if ji in live]
+                    if not members:
+                        continue
+                    d, total, counter, shp = self._pass_descs(p, members)
+                    side = self._side[gi % len(self._side)]
+                    _lib.check(self.L.par2cuda_batch_muladd(d.data_ptr(), len(members), total, counter.data_ptr(), shp,
+                                                            side.cuda_stream), "batch_muladd")
+            else:
+                # each job's grid launch (largest first), round-robin over the side streams
+                for k, ji in enumerate(live):
+                    self._muladd_grid(self.bufs[ji], p, self._side[k % len(self._side)].cuda_stream)
+            for side in self._side:
+                cur.wait_stream(side)
             for ji in live:
                 self._verify(self.bufs[ji], p, st)
                 if verify_cb:
                     verify_cb(self.bufs[ji], p)
+
+    def tune_mode(self):
+        """Times the multiply-accumulate of pass 0 in each mode (eagerly, after
+        one untimed run of each) and keeps the faster; returns the times (ms)."""
+        cur = torch.cuda.current_stream(self.dev)
+        st = cur.cuda_stream
+        live = [ji for ji, b in enumerate(self.bufs) if b.window(0)[1] > 0]
+        for ji in live:
+            self._window_prep(self.bufs[ji], 0, st)
+        times = {}
+        for mode in self.MODES:
+            for rep in range(2):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(cur)
+                for side in self._side:
+                    side.wait_stream(cur)
+                if mode == "persistent":
+                    groups = {}
+                    for ji in live:
+                        groups.setdefault(self.shapes[ji], []).append(ji)
+                    for gi, (shape, members) in enumerate(sorted(groups.items())):
+                        d, total, counter, shp = self._pass_descs(0, members)
+                        _lib.check(self.L.par2cuda_batch_muladd(d.data_ptr(), len(members), total, counter.data_ptr(),
+                                                                shp, self._side[gi % len(self._side)].cuda_stream), "batch")
+                else:
+                    for k, ji in enumerate(live):
+                        self._muladd_grid(self.bufs[ji], 0, self._side[k % len(self._side)].cuda_stream)
+                for side in self._side:
+                    cur.wait_stream(side)
+                e1.record(cur)
+                e1.synchronize()
+                times[mode] = e0.elapsed_time(e1)
+        self.mode = min(times, key=times.get)
+        self.graph = None
+        return times
 
     def capture(self):
         """Runs the batched sequence once eagerly (one-time set-up), then

@@ -599,50 +599,235 @@ __global__ void __launch_bounds__((NL + 4) * 32, 1) k_comb_pair(
 	pair_unit<RPW, NL, GP>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate, tile, rb * (RPW * NL), 0u, smem);
 }
 
-// Persistent batched form of the paired kernel: as k_comb_batched, one CTA
-// per SM takes (job, word tile, recovery block) units from an atomic ticket.
-// The mbarrier ring runs on across units (global slot numbering); a
-// __syncthreads separates units, and a unit whose bounded wait gave up stops
-// the CTA for good (every thread leaves the loop at the same barrier).
+// Persistent batched form of the paired kernel: one CTA per SM takes (job,
+// word tile, recovery block) units from an atomic ticket.  The builder warps
+// own the ticket and run ahead across unit boundaries: every ring slot
+// carries a small descriptor (job, recovery block, word tile, row count,
+// first/last flags, or the end marker), so the lookup warps start a unit's
+// accumulators at its first slot and write its recovery words after its last
+// slot, and no CTA-wide barrier separates units.  Unit-boundary latency is
+// hidden on the builder side: the job table (up to 64 jobs) is cached in
+// shared memory, the next ticket is taken one unit ahead, and the next
+// unit's first inputs are fetched while the current unit's last slot is
+// consumed.  All waits are bounded: a builder whose wait gave up stops doing
+// work and the builder group leaves together at its next group barrier;
+// lookup warps stop at their next wait.
+struct SlotMeta { unsigned long long tile; unsigned job, rbase, flags, R; };
+enum { SLOT_FIRST = 1u, SLOT_LAST = 2u, SLOT_END = 4u };
+struct UnitRef { unsigned long long tile; unsigned job, rbase, end, pad; };
+constexpr int BATCH_CACHED_JOBS = 64;
+
+__device__ __forceinline__ void builders_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
 template<int RPW, int NL, int GP>
 __global__ void __launch_bounds__((NL + 4) * 32, 1) k_comb_pair_batched(
 	const BatchJob* __restrict__ jobs, unsigned nJobs, unsigned long long totalUnits,
 	unsigned long long* __restrict__ counter)
 {
+	static_assert(GP == 1 || GP == 2, "one or two tables per slot");
 	constexpr int RT = RPW * NL;
+	constexpr int TBL = 65536;
+	constexpr int NJ = (RT * GP + 127) / 128;
 	extern __shared__ __align__(16) uint8_t smem[];
-	__shared__ unsigned long long s_unit;
-	__shared__ unsigned s_job;
-	__shared__ int s_abort;
+	uint8_t* tbl = smem;
+	uint4* idxs = reinterpret_cast<uint4*>(smem + GP * TBL);                  // [2][GP][RT]
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + GP * TBL + 2 * GP * RT * sizeof(uint4));
+	__shared__ SlotMeta meta[2];
+	__shared__ UnitRef s_unit[2];
+	__shared__ BatchJob s_jobs[BATCH_CACHED_JOBS];
+	__shared__ int s_babort;
+
+	const bool cached = nJobs <= BATCH_CACHED_JOBS;
 	pair_init_bars<RPW, NL, GP>(smem);
-	if(threadIdx.x == 0) s_abort = 0;
+	if(threadIdx.x == 0) s_babort = 0;
+	if(cached)
+		for(unsigned j = threadIdx.x; j < nJobs; j += blockDim.x) s_jobs[j] = jobs[j];
 	__syncthreads();
-	unsigned gs = 0;
-	for(;;) {
-		if(threadIdx.x == 0) {
-			unsigned long long u = atomicAdd(counter, 1ull);
-			s_unit = u;
+	const BatchJob* JT = cached ? s_jobs : jobs;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+	if(warp >= NL) {
+		// ---------------- builders (4 warps, 128 threads)
+		const int bw = warp - NL;
+		const int bt = threadIdx.x - NL * 32;
+		auto decode = [&](unsigned long long u) {
+			UnitRef r;
+			r.pad = 0;
+			if(u >= totalUnits) { r.end = 1; r.job = 0; r.tile = 0; r.rbase = 0; return r; }
 			unsigned lo = 0, hi = nJobs;
 			while(hi - lo > 1) {
-				unsigned mid = (lo + hi) >> 1;
-				if(jobs[mid].unitBase <= u) lo = mid; else hi = mid;
+				const unsigned mid = (lo + hi) >> 1;
+				if(JT[mid].unitBase <= u) lo = mid; else hi = mid;
 			}
-			s_job = lo;
+			const unsigned rblocks = (JT[lo].R + RT - 1) / RT;
+			const unsigned long long local = u - JT[lo].unitBase;
+			r.end = 0; r.job = lo; r.tile = local / rblocks; r.rbase = (unsigned)(local % rblocks) * RT;
+			return r;
+		};
+		unsigned long long tnext = 0;
+		if(bt == 0) {
+			s_unit[0] = decode(atomicAdd(counter, 1ull));
+			tnext = atomicAdd(counter, 1ull);
 		}
-		__syncthreads();
-		const unsigned long long u = s_unit;
-		if(u >= totalUnits || s_abort) break;
-		const BatchJob& J = jobs[s_job];
-		const unsigned long long local = u - J.unitBase;
-		const unsigned rblocks = (J.R + RT - 1) / RT;
-		const size_t tile = (size_t)(local / rblocks);
-		const unsigned rb = (unsigned)(local % rblocks);
-		const unsigned G = (J.nIn + 7) / 8;
-		if(!pair_unit<RPW, NL, GP>(J.in, J.inPitch, J.nIn, J.idx, G, J.rec, J.recPitch, J.R, J.accumulate,
-		                           tile, rb * RT, gs, smem))
-			s_abort = 1;
-		gs += (G + GP - 1) / GP;
-		__syncthreads(); // s_unit / s_job are rewritten next round
+		builders_sync();
+		UnitRef cur = s_unit[0], nxt = cur;
+
+		uint32_t x[GP][8];
+		uint4 ip[NJ];
+		auto fetch = [&](const UnitRef& ur, unsigned s) {
+			const BatchJob& J = JT[ur.job];
+			const unsigned nIn = J.nIn, R = J.R, G = (nIn + 7) / 8;
+			const size_t colWord = (size_t)ur.tile * P2C_TILE_WORDS + lane * 2;
+#pragma unroll
+			for(int t = 0; t < GP; t++)
+#pragma unroll
+				for(int v = 0; v < 8; v++) {
+					const unsigned i = (s * GP + t) * 8 + v;
+					x[t][v] = i < nIn ? __ldg(reinterpret_cast<const uint32_t*>(J.in + (size_t)i * J.inPitch + colWord)) : 0u;
+				}
+#pragma unroll
+			for(int q = 0; q < NJ; q++) {
+				const int jj = bt + q * 128;
+				ip[q] = make_uint4(0, 0, 0, 0);
+				if(jj < GP * RT) {
+					const int t = jj / RT, j = jj - t * RT;
+					const unsigned g = s * GP + t, r = ur.rbase + j;
+					if(g < G && r < R) ip[q] = __ldg(J.idx + (size_t)r * G + g);
+				}
+			}
+		};
+
+		unsigned gs = 0;
+		bool dead = false, prefetched = false;
+		for(unsigned k = 0;; ++k) {
+			if(cur.end) {                       // end marker slot
+				const int b = gs & 1;
+				if(dead || (gs >= 2 && !mbar_wait(&bars[2 + b], ((gs >> 1) - 1) & 1))) return;
+				if(bt == 0) meta[b].flags = SLOT_END;
+				mbar_arrive(&bars[b]);
+				return;
+			}
+			const unsigned R = JT[cur.job].R;
+			const unsigned G = (JT[cur.job].nIn + 7) / 8;
+			const unsigned NS = G ? (G + GP - 1) / GP : 1;   // a job without inputs sends one zero slot
+			if(!dead && !prefetched) fetch(cur, 0);
+			prefetched = false;
+			for(unsigned s = 0; s < NS; s++) {
+				const int b = gs & 1;
+				if(!dead && gs >= 2 && !mbar_wait(&bars[2 + b], ((gs >> 1) - 1) & 1)) { dead = true; s_babort = 1; }
+				if(!dead) {
+#pragma unroll
+					for(int t = 0; t < GP; t++) {
+						uint8_t* base = tbl + t * TBL + b * 128 + lane * 4;
+#pragma unroll
+						for(int hh = 0; hh < 4; hh++) {
+							const int h = bw * 4 + hh;
+							uint32_t v = 0;
+#pragma unroll
+							for(int w = 0; w < 4; w++) if(h >> w & 1) v ^= x[t][4 + w];
+							uint8_t* rowp = base + h * 16 * 256;
+							*reinterpret_cast<uint32_t*>(rowp) = v;
+#pragma unroll
+							for(int n = 1; n < 16; n++) {
+								const int gray = n ^ (n >> 1);
+								const int bit = (n & 1) ? 0 : (n & 2) ? 1 : (n & 4) ? 2 : 3;
+								v ^= x[t][bit];
+								*reinterpret_cast<uint32_t*>(rowp + gray * 256) = v;
+							}
+						}
+					}
+#pragma unroll
+					for(int q = 0; q < NJ; q++) {
+						const int jj = bt + q * 128;
+						if(jj < GP * RT) idxs[b * GP * RT + jj] = ip[q];
+					}
+					if(bt == 0) {
+						SlotMeta m;
+						m.tile = cur.tile; m.job = cur.job; m.rbase = cur.rbase; m.R = R;
+						m.flags = (s == 0 ? SLOT_FIRST : 0u) | (s + 1 == NS ? SLOT_LAST : 0u);
+						meta[b] = m;
+					}
+					mbar_arrive(&bars[b]);
+				}
+				++gs;
+				if(s == 0) {
+					// publish the next unit (its ticket was taken one unit ago)
+					if(bt == 0) {
+						s_unit[(k + 1) & 1] = decode(tnext);
+						if(tnext < totalUnits) tnext = atomicAdd(counter, 1ull);
+					}
+					builders_sync();
+					if(s_babort) return;
+					nxt = s_unit[(k + 1) & 1];
+				}
+				if(dead) continue;
+				if(s + 1 < NS) fetch(cur, s + 1);
+				else if(!nxt.end) { fetch(nxt, 0); prefetched = true; }
+			}
+			cur = nxt;
+		}
+	}
+
+	// ---------------- lookups
+	uint32_t acc[RPW][16];
+#pragma unroll
+	for(int s = 0; s < RPW; s++)
+#pragma unroll
+		for(int k = 0; k < 16; k++) acc[s][k] = 0;
+	const uint32_t lwb = (uint32_t)lane * 4;
+	for(unsigned gs = 0;; ++gs) {
+		const int b = gs & 1;
+		if(!mbar_wait(&bars[b], (gs >> 1) & 1)) return;
+		// only the flags are live during the lookups; the rest of the slot
+		// descriptor is read after them, before the slot is released
+		const unsigned flags = meta[b].flags;
+		if(flags & SLOT_END) return;
+		if(flags & SLOT_FIRST) {
+#pragma unroll
+			for(int s = 0; s < RPW; s++)
+#pragma unroll
+				for(int k = 0; k < 16; k++) acc[s][k] = 0;
+		}
+		const uint32_t lw = lwb + b * 128;
+		// no per-row guard: rows past R have zero index rows (staged by the
+		// builders), so their lookups read table row 0 (= 0)
+#pragma unroll
+		for(int s = 0; s < RPW; s++) {
+			const int j = warp * RPW + s;
+			uint32_t qq[GP][4];
+#pragma unroll
+			for(int t = 0; t < GP; t++) {
+				const uint4 q = idxs[(b * GP + t) * RT + j];
+				qq[t][0] = q.x; qq[t][1] = q.y; qq[t][2] = q.z; qq[t][3] = q.w;
+			}
+#pragma unroll
+			for(int k = 0; k < 16; k++) {
+				const uint32_t sel = 4u | ((uint32_t)(k & 3) << 4) | (5u << 8) | (5u << 12);
+				uint32_t v = *reinterpret_cast<const uint32_t*>(tbl + __byte_perm(qq[0][k >> 2], lw, sel));
+				if(GP == 2) v ^= *reinterpret_cast<const uint32_t*>(tbl + TBL + __byte_perm(qq[GP - 1][k >> 2], lw, sel));
+				acc[s][k] ^= v;
+			}
+		}
+		SlotMeta m = {};
+		if(flags & SLOT_LAST) m = meta[b];
+		__syncwarp();
+		if(lane == 0) mbar_arrive(&bars[2 + b]);   // slot (tables, index rows, descriptor) released
+		if(flags & SLOT_LAST) {
+			const BatchJob& J = JT[m.job];
+			const size_t colWord = (size_t)m.tile * P2C_TILE_WORDS + lane * 2;
+#pragma unroll
+			for(int s = 0; s < RPW; s++) {
+				const unsigned r = m.rbase + warp * RPW + s;
+				if(r < m.R) {
+					uint32_t v = acc[s][15];
+#pragma unroll
+					for(int k = 14; k >= 0; k--) v = mul2x2(v) ^ acc[s][k];
+					uint32_t* p = reinterpret_cast<uint32_t*>(J.rec + (size_t)r * J.recPitch + colWord);
+					if(J.accumulate) v ^= *p;
+					*p = v;
+				}
+			}
+		}
 	}
 }
 
