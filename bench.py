@@ -389,6 +389,62 @@ def run_ours(args, cfg, file_lens):
                       "path": "C ABI plugin calls from the host: wait_for_add + add_input x N (pinned host slices), "
                               "end_input, get_output x R (verdict callbacks); GF multiply-accumulate + internal "
                               "checksum, no hashing (the reference plugin does not hash); host wall clock"}
+    # several independent jobs in flight: job k runs its whole pass on its own
+    # context stream with its own seeded inputs, so one job's per-file MD5
+    # chains (serial, ~100 MB/s per GPU thread) overlap the others' work;
+    # each job's steps stay in order on its stream
+    inflight = None
+    if args.inflight > 1 and cfg["hashes"]:
+        jobs_k = [job] + [ResidentJob(S, file_lens, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
+                          for _ in range(args.inflight - 1)]
+        for k, jk in enumerate(jobs_k[1:], 1):
+            jk.fill_synthetic(seed=1 + rank + 1000 * k)
+        ctx = [torch.cuda.Stream(device=dev) for _ in jobs_k]
+        cur = torch.cuda.current_stream(dev)
+
+        def round_(upload=None, down=None):
+            for k, jk in enumerate(jobs_k):
+                ctx[k].wait_stream(cur)
+                with torch.cuda.stream(ctx[k]):
+                    if upload is not None:
+                        jk.upload(upload)
+                    jk.run(hashes=True)
+                    if down is not None:
+                        jk.download(down[k])
+            for c in ctx:
+                cur.wait_stream(c)
+        round_()
+        torch.cuda.synchronize()
+        i0 = torch.cuda.Event(enable_timing=True)
+        i1 = torch.cuda.Event(enable_timing=True)
+        i0.record()
+        for _ in range(args.steps):
+            round_()
+        i1.record()
+        torch.cuda.synchronize()
+        ims = max_over_ranks(i0.elapsed_time(i1) / args.steps)
+        assert all(int(jk.d_flags.sum()) == R for jk in jobs_k)
+        inflight = {"jobs_in_flight": len(jobs_k), "value": mul_adds * len(jobs_k) * world / (ims / 1e3), "unit": UNIT,
+                    "ms_per_round": ims, "jobs_per_s": len(jobs_k) * world / (ims / 1e3),
+                    "desc": "%d independent jobs of this workload (distinct seeded inputs, each resident) per round, "
+                            "each on its own stream; whole pass per job incl. IFSC + file MD5" % len(jobs_k)}
+        if e2e is not None:
+            downs = [torch.empty((R, S), dtype=torch.uint8, pin_memory=True) for _ in jobs_k]
+            round_(host_in, downs)
+            torch.cuda.synchronize()
+            i0.record()
+            for _ in range(args.steps):
+                round_(host_in, downs)
+            i1.record()
+            torch.cuda.synchronize()
+            ems_k = max_over_ranks(i0.elapsed_time(i1) / args.steps)
+            inflight["e2e"] = {"value": mul_adds * len(jobs_k) * world / (ems_k / 1e3), "unit": UNIT,
+                               "ms_per_round": ems_k, "h2d_bytes_per_round": N * S * len(jobs_k),
+                               "d2h_bytes_per_round": job.d2h_bytes() * len(jobs_k)}
+            del downs
+        del jobs_k
+        torch.cuda.empty_cache()
+
     stop.set()
     if th:
         th.join(timeout=3)
@@ -436,6 +492,7 @@ def run_ours(args, cfg, file_lens):
         "clocks": clocks,
         "e2e": e2e,
         "e2e_plugin": e2e_plugin,
+        "inflight": inflight,
     }
     if args.traffic_bytes:
         line["roofline"]["traffic"] = args.traffic_bytes
@@ -480,6 +537,37 @@ def run_serving_workload(args, cfg):
     }
     print(json.dumps(line))
     return 0
+
+
+def small_mix_run(args):
+    """Supplement to the 64-job mix: 512 small jobs (N log-uniform [10, 200],
+    S 64 KiB..1 MiB, R 1-30 % of N), where per-job launches leave the GPU
+    partly idle; per-job launches vs the tuned batched graph."""
+    import torch
+    from parpar_gb300.batch import BatchRunner, make_job_mix
+    jobs = make_job_mix(512, seed=6, n_range=(10, 200), s_range=(64 * 1024, 1 << 20))
+    runner = BatchRunner(jobs, budget_bytes=args.budget_gib << 30)
+    runner.run_per_job()
+    t0 = time.perf_counter()
+    runner.run_per_job()
+    t_job = time.perf_counter() - t0
+    modes = runner.tune_mode()
+    runner.capture()
+    for _ in range(max(args.warmup, 1)):
+        runner.run_batched()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        runner.run_batched()
+    e1.record()
+    torch.cuda.synchronize()
+    assert runner.all_valid()
+    ms = e0.elapsed_time(e1) / args.steps
+    return {"jobs": len(jobs), "mul_adds": runner.mul_adds, "passes": runner.P,
+            "batched_jobs_per_s": len(jobs) / (ms / 1e3), "per_job_jobs_per_s": len(jobs) / t_job,
+            "speedup_vs_per_job_launch": t_job / (ms / 1e3), "batched_mode": runner.mode, "mode_pass0_ms": modes}
 
 
 def run_batched_workload(args, cfg):
@@ -533,6 +621,7 @@ def run_batched_workload(args, cfg):
                            "p50_job_s": float(np.percentile(lat, 50)), "p99_job_s": float(np.percentile(lat, 99))},
         "speedup_vs_per_job_launch": (len(jobs) / (ms / 1e3)) / (len(jobs) / t_job),
         "batched_mode": runner.mode, "mode_pass0_ms": mode_ms,
+        "small_jobs_mix": small_mix_run(args),
         "autotune": {str(k): v[0] for k, v in autotune.table().items()},
         "gpu_launches": runner.launches_per_run() * args.steps,
         "clocks": summarize_clocks(clock_lines, 0),
@@ -557,6 +646,8 @@ def main():
     ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor"], default="comb",
                     help="multiply-accumulate kernel of the resident-job workloads")
     ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")
+    ap.add_argument("--inflight", type=int, default=8,
+                    help="independent jobs in flight for the multi-job figure of hashing workloads (0/1 = skip)")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline.traffic")
     args = ap.parse_args()

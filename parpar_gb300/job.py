@@ -115,7 +115,11 @@ class ResidentJob:
         self.d_ifsc = torch.empty(self.N * 20, dtype=torch.uint8, device=dev)
         self.d_fmd5 = torch.empty(len(self.file_lens) * 16, dtype=torch.uint8, device=dev)
         self.sa = stream_a or torch.cuda.Stream(device=dev)
-        self.sb = stream_b or torch.cuda.Stream(device=dev)
+        # the per-file MD5 chains run for the whole job on a few threads: their
+        # stream gets the highest priority so that their CTAs are dispatched as
+        # soon as an SM frees, ahead of pending multiply-accumulate CTAs of
+        # other jobs in flight
+        self.sb = stream_b or torch.cuda.Stream(device=dev, priority=-10)
         self.launches_per_run = 8
 
     # -------------------------------------------------------------- inputs
