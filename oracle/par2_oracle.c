@@ -257,6 +257,8 @@ static void or_md5_block(uint32_t* st, const uint8_t* blk) {
 	for(int i = 0; i < 16; i++)
 		m[i] = (uint32_t)blk[4*i] | ((uint32_t)blk[4*i+1] << 8) | ((uint32_t)blk[4*i+2] << 16) | ((uint32_t)blk[4*i+3] << 24);
 	uint32_t a = st[0], b = st[1], c = st[2], d = st[3];
+	/* fully unrolled, so the round constants and rotations fold into the code */
+#pragma GCC unroll 64
 	for(int i = 0; i < 64; i++) {
 		uint32_t f; int g;
 		if(i < 16) { f = (b & c) | (~b & d); g = i; }
