@@ -263,6 +263,15 @@ unsigned long long par2cuda_batch_units(unsigned num_rec, size_t n_words, int sh
 /* One persistent launch over d_jobs[0..num_jobs) (device array). */
 int par2cuda_batch_muladd(const par2cuda_batch_job* d_jobs, unsigned num_jobs, unsigned long long total_units,
                           unsigned long long* d_counter, int shape, void* stream);
+/* Multiply-accumulate of one job from index bytes prepared once
+ * (par2cuda_coeff_index or par2cuda_par2_index), as a grid launch of the
+ * automatic comb shape: d_rec[r] (^)= sum_i c(r,i) d_in[i] over n_words words.
+ * Pitches are in 16-bit words and at least roundup(n_words, 64).  No
+ * counterpart in the reference (its kernels take coefficients per call); it
+ * serves callers that keep a job's index resident across chunks. */
+int par2cuda_muladd_index(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in, const void* d_index,
+                          uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec, size_t n_words, int accumulate,
+                          void* stream);
 
 #ifdef __cplusplus
 }

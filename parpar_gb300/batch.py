@@ -150,11 +150,18 @@ class BatchRunner:
         return ((n_bytes + 7) // 8 * 8 + 8) // 2
 
     def _muladd_grid(self, b: _JobBufs, p: int, st):
-        """One job's window through the single-job C-ABI call (grid launch)."""
+        """One job's window through the single-job C-ABI call (grid launch;
+        converts the coefficients to index bytes in its scratch each call)."""
         off, n = b.window(p)
         _lib.check(self.L.par2cuda_muladd(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_coeff.data_ptr(), b.d_rec.data_ptr(),
                                           b.pw, b.spec.R, self._n_words(n), 0, _lib.METHOD_COMB, b.d_idx.data_ptr(),
                                           b.d_idx.numel(), st), "muladd")
+
+    def _muladd_index(self, b: _JobBufs, p: int, st):
+        """One job's window as a grid launch from its resident index bytes."""
+        off, n = b.window(p)
+        _lib.check(self.L.par2cuda_muladd_index(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_idx.data_ptr(), b.d_rec.data_ptr(),
+                                                b.pw, b.spec.R, self._n_words(n), 0, st), "muladd_index")
 
     # ------------------------------------------------------------ per-job path
     def run_per_job(self, verify_cb=None):
@@ -234,7 +241,7 @@ class BatchRunner:
             else:
                 # each job's grid launch (largest first), round-robin over the side streams
                 for k, ji in enumerate(live):
-                    self._muladd_grid(self.bufs[ji], p, self._side[k % len(self._side)].cuda_stream)
+                    self._muladd_index(self.bufs[ji], p, self._side[k % len(self._side)].cuda_stream)
             for side in self._side:
                 cur.wait_stream(side)
             for ji in live:
@@ -268,7 +275,7 @@ class BatchRunner:
                                                                 shp, self._side[gi % len(self._side)].cuda_stream), "batch")
                 else:
                     for k, ji in enumerate(live):
-                        self._muladd_grid(self.bufs[ji], 0, self._side[k % len(self._side)].cuda_stream)
+                        self._muladd_index(self.bufs[ji], 0, self._side[k % len(self._side)].cuda_stream)
                 for side in self._side:
                     cur.wait_stream(side)
                 e1.record(cur)

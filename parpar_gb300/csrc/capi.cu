@@ -236,4 +236,17 @@ int par2cuda_batch_muladd(const par2cuda_batch_job* d_jobs, unsigned num_jobs, u
 	                         (cudaStream_t)stream);
 }
 
+int par2cuda_muladd_index(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in, const void* d_index,
+                          uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec, size_t n_words, int accumulate,
+                          void* stream) {
+	if(!num_rec || !n_words) return 0;
+	if((!d_in && num_in) || !d_rec || (!d_index && num_in)) { p2c::set_error("muladd_index: null pointer"); return -1; }
+	if(in_pitch_words < p2c::round_up(n_words, P2C_TILE_WORDS) || rec_pitch_words < p2c::round_up(n_words, P2C_TILE_WORDS)) {
+		p2c::set_error("muladd_index: row pitch below roundup(n_words, 64)");
+		return -1;
+	}
+	return p2c::comb_muladd(d_in, in_pitch_words, num_in, reinterpret_cast<const uint4*>(d_index), d_rec, rec_pitch_words,
+	                        num_rec, n_words, accumulate, 0, (cudaStream_t)stream);
+}
+
 } // extern "C"

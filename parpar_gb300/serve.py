@@ -51,8 +51,9 @@ def poisson_arrivals(n: int, rate: float, seed: int) -> np.ndarray:
 
 class Server:
     def __init__(self, budget_bytes: int = 150 * 10**9, slots: int = 8, device: int = 0, digests: bool = False,
-                 chunk_share: float = 0.5):
+                 chunk_share: float = 0.5, persistent: bool = False):
         self.L = _lib.load()
+        self.persistent = persistent     # persistent batch launch per chunk instead of a grid launch
         self.dev = torch.device("cuda", device)
         self.budget = budget_bytes
         self.slots = slots
@@ -97,7 +98,7 @@ class Server:
             d_flags = torch.zeros(spec.R, dtype=torch.uint8, device=self.dev)
             d_ok = torch.ones(1, dtype=torch.uint8, device=self.dev)
             counter = torch.zeros(1, dtype=torch.int64, device=self.dev)
-        shape = autotune.best_shape(spec.R)
+        shape = autotune.best_shape(spec.R) if self.persistent else 0
         _lib.check(L.par2cuda_par2_index(d_nums.data_ptr(), spec.N, d_exps.data_ptr(), spec.R, d_idx.data_ptr(), st), "index")
         n_pass = math.ceil(spec.S / W)
         descs = []
@@ -108,11 +109,17 @@ class Server:
             nw = ((n + 7) // 8 * 8 + 8) // 2
             _lib.check(L.par2cuda_synth_fill_at(d_in.data_ptr(), pitch, spec.N, n, spec.seed, 0, off, st), "synth")
             _lib.check(L.par2cuda_rows_checksum(d_in.data_ptr(), pw, spec.N, None, n, 0, None, d_ck.data_ptr(), st), "cksum")
-            jd = _lib.BatchJob(d_in.data_ptr(), pw, spec.N, d_idx.data_ptr(), d_rec.data_ptr(), pw, spec.R, 0, 0)
-            units = L.par2cuda_batch_units(spec.R, nw, shape)
-            dd = torch.frombuffer(bytearray(jd), dtype=torch.uint8).to(self.dev)
-            descs.append(dd)
-            _lib.check(L.par2cuda_batch_muladd(dd.data_ptr(), 1, units, counter.data_ptr(), shape, st), "muladd")
+            if self.persistent:
+                jd = _lib.BatchJob(d_in.data_ptr(), pw, spec.N, d_idx.data_ptr(), d_rec.data_ptr(), pw, spec.R, 0, 0)
+                units = L.par2cuda_batch_units(spec.R, nw, shape)
+                dd = torch.frombuffer(bytearray(jd), dtype=torch.uint8).to(self.dev)
+                descs.append(dd)
+                _lib.check(L.par2cuda_batch_muladd(dd.data_ptr(), 1, units, counter.data_ptr(), shape, st), "muladd")
+            else:
+                # grid launch from the resident index bytes (measured faster than
+                # the persistent launch on GB300)
+                _lib.check(L.par2cuda_muladd_index(d_in.data_ptr(), pw, spec.N, d_idx.data_ptr(), d_rec.data_ptr(), pw,
+                                                   spec.R, nw, 0, st), "muladd")
             _lib.check(L.par2cuda_rows_checksum(d_rec.data_ptr(), pw, spec.R, None, n, 1, d_flags.data_ptr(),
                                                d_ck.data_ptr(), st), "verify")
             with torch.cuda.stream(st_obj):

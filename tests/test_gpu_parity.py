@@ -329,3 +329,40 @@ def test_lop3_rate_calibration():
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     per_sm_clk = v.value / sms / 2.0e9
     assert 16 < per_sm_clk < 300, v.value
+
+
+def test_muladd_index_matches_oracle():
+    """par2cuda_muladd_index (grid launch from resident index bytes) over
+    chunks of one job: accumulate mode and the device-computed PAR2 index."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    n, R, S = 45, 77, 5000
+    d_in, pw = _dev_rows(torch, n, S, 4242)
+    host_in = synth.slices(4242, 0, n, S)
+    exps = list(range(3, 3 + R))
+    d_nums = torch.arange(n, dtype=torch.int16, device="cuda")
+    d_exps = torch.tensor(np.asarray(exps, dtype=np.uint16).view(np.int16), device="cuda")
+    d_idx = torch.zeros(L.par2cuda_coeff_index_bytes(R, n), dtype=torch.uint8, device="cuda")
+    _lib.check(L.par2cuda_par2_index(d_nums.data_ptr(), n, d_exps.data_ptr(), R, d_idx.data_ptr(), None), "index")
+    want = O.recover(host_in, np.full(n, S), np.arange(n), exps)
+    d_rec = torch.zeros((R, pw), dtype=torch.int16, device="cuda")
+    nw = S // 2
+    # two halves of the inputs, the second accumulating
+    h = 24
+    idx_a = torch.zeros(L.par2cuda_coeff_index_bytes(R, h), dtype=torch.uint8, device="cuda")
+    idx_b = torch.zeros(L.par2cuda_coeff_index_bytes(R, n - h), dtype=torch.uint8, device="cuda")
+    _lib.check(L.par2cuda_par2_index(d_nums[:h].data_ptr(), h, d_exps.data_ptr(), R, idx_a.data_ptr(), None), "ia")
+    _lib.check(L.par2cuda_par2_index(d_nums[h:].data_ptr(), n - h, d_exps.data_ptr(), R, idx_b.data_ptr(), None), "ib")
+    _lib.check(L.par2cuda_muladd_index(d_in.data_ptr(), pw, h, idx_a.data_ptr(), d_rec.data_ptr(), pw, R, nw, 0, None), "a")
+    _lib.check(L.par2cuda_muladd_index(d_in[h:].data_ptr(), pw, n - h, idx_b.data_ptr(), d_rec.data_ptr(), pw, R, nw, 1,
+                                       None), "b")
+    torch.cuda.synchronize()
+    assert np.array_equal(d_rec.cpu().numpy().view(np.uint8)[:, :S], want)
+    # whole job in one call
+    d_rec.zero_()
+    _lib.check(L.par2cuda_muladd_index(d_in.data_ptr(), pw, n, d_idx.data_ptr(), d_rec.data_ptr(), pw, R, nw, 0, None), "w")
+    torch.cuda.synchronize()
+    assert np.array_equal(d_rec.cpu().numpy().view(np.uint8)[:, :S], want)
+    assert L.par2cuda_device_error() == 0
+    # pitch below roundup(n_words, 64) is rejected
+    assert L.par2cuda_muladd_index(d_in.data_ptr(), 32, n, d_idx.data_ptr(), d_rec.data_ptr(), pw, R, nw, 0, None) < 0

@@ -20,12 +20,12 @@ def _oracle_digest(spec, window):
     return h.hexdigest()
 
 
-@pytest.mark.parametrize("chunk_share", [0.5, 0.02])
-def test_serving_alone_equals_mix(chunk_share):
+@pytest.mark.parametrize("chunk_share,persistent", [(0.5, False), (0.02, False), (0.5, True), (0.02, True)])
+def test_serving_alone_equals_mix(chunk_share, persistent):
     pytest.importorskip("torch")
     from parpar_gb300.serve import Request, Server, make_requests
     reqs = make_requests(12, rate=2000.0, seed=7, n_range=(3, 80), s_range=(64, 20000), r_frac=(0.05, 0.5))
-    mk = lambda: Server(budget_bytes=3 * 10**6, slots=3, digests=True, chunk_share=chunk_share)
+    mk = lambda: Server(budget_bytes=3 * 10**6, slots=3, digests=True, chunk_share=chunk_share, persistent=persistent)
     srv = mk()
     done = srv.run(reqs)
     assert len(done) == len(reqs)
