@@ -33,6 +33,10 @@ sys.path.insert(0, ROOT)
 METRIC = "GF16 mul-adds/s"
 UNIT = "mul-adds/s"
 
+# one ncu capture of k_comb_pair<6,12,2> (512 inputs x 200 recovery x 512 KiB):
+# dram__bytes_read.sum + dram__bytes_write.sum, and the algorithmic (N + R) x S
+PAIR_TRAFFIC = (270406912 + 87077120, (512 + 200) * 524288)
+
 WORKLOADS = {
     # name: (slice bytes, input slices, files, recovery slices, hashing)
     "bandwidth": dict(S=2 * 1048576, N=2000, files=40, R=200, hashes=True,
@@ -292,9 +296,14 @@ def run_ours(args, cfg, file_lens):
         step()
     torch.cuda.synchronize()
     assert int(job.d_flags.sum()) == R, "recovery checksum verification failed"
-    # integer-ALU roofline denominator: the device's measured LOP3 rate
+    # roofline denominators measured on this device: the LOP3 rate (integer-ALU
+    # bound of the contraction) and one MD5 chain's rate on one thread (the
+    # latency bound of the one-stream-per-thread hash kernels)
     lop3 = ctypes.c_double(0)
     _lib.check(L.par2cuda_lop3_rate(ctypes.byref(lop3), None), "lop3_rate")
+    md5_chain = ctypes.c_double(0)
+    if cfg["hashes"]:
+        _lib.check(L.par2cuda_md5_chain_rate(ctypes.byref(md5_chain), None), "md5_chain_rate")
     torch.cuda.synchronize()
 
     clock_lines, stop = [], threading.Event()
@@ -488,7 +497,7 @@ def run_ours(args, cfg, file_lens):
         "src_GBps_x_recovery": N * S * R * world / (ms / 1e3) / 1e9,
         "kernels_ms": {"muladd": comb_ms, "file_md5": hash_ms, "step": ms},
         "method": args.method,
-        "roofline": {"bound": "int-alu", "kernel": kname, "achieved": 2 * comb_rate / 1e12,
+        "roofline_gf": {"bound": "int-alu", "kernel": kname, "achieved": 2 * comb_rate / 1e12,
                      "peak": alu_peak, "unit": "Tops/s", "frac": 2 * comb_rate / 1e12 / alu_peak,
                      "traffic": None, "alg_bytes": alg_bytes,
                      "peak_source": "measured: LOP3 calibration kernel k_lop3_rate on this GPU (%.1f lanes/SM/clk at "
@@ -505,7 +514,24 @@ def run_ours(args, cfg, file_lens):
         "inflight": inflight,
     }
     if args.traffic_bytes:
-        line["roofline"]["traffic"] = args.traffic_bytes
+        line["roofline_gf"]["traffic"] = args.traffic_bytes
+    elif kname == "k_comb_pair":
+        # DRAM bytes per launch scaled from the ncu capture of the same kernel
+        # on 512 x 200 x 512 KiB (profiles/comb_pair_512x200x512KiB.md):
+        # inputs are read once and recovery rows written once, so traffic grows
+        # with (N + R) x S
+        line["roofline_gf"]["traffic"] = PAIR_TRAFFIC[0] / PAIR_TRAFFIC[1] * alg_bytes
+        line["roofline_gf"]["traffic_source"] = "ncu dram__bytes_read+write of k_comb_pair<6,12,2> on 512x200x512KiB " \
+            "(%.1f MB for %.1f MB algorithmic), scaled by (N+R)*S" % (PAIR_TRAFFIC[0] / 1e6, PAIR_TRAFFIC[1] / 1e6)
+    if cfg["hashes"]:
+        big = max(file_lens)
+        line["roofline_md5"] = {
+            "bound": "latency", "kernel": "k_file_md5", "achieved": big / (hash_ms / 1e3) / 1e6,
+            "peak": md5_chain.value / 1e6, "unit": "MB/s per GPU thread (largest file's chain)",
+            "frac": big / (hash_ms / 1e3) / md5_chain.value, "traffic": None,
+            "peak_source": "measured: k_md5_chain, one MD5 stream on one thread with its data in registers"}
+    # `roofline` is the kernel that bounds the step (the longest live kernel time)
+    line["roofline"] = dict(line["roofline_md5"] if cfg["hashes"] and hash_ms > comb_ms else line["roofline_gf"])
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1, window=args.cpu_window)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "method")}
@@ -659,7 +685,7 @@ def main():
     ap.add_argument("--inflight", type=int, default=8,
                     help="independent jobs in flight for the multi-job figure of hashing workloads (0/1 = skip)")
     ap.add_argument("--traffic-bytes", type=float, default=None,
-                    help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline.traffic")
+                    help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline_gf.traffic")
     args = ap.parse_args()
     cfg = WORKLOADS[args.workload]
     if args.workload in ("batched", "serving"):

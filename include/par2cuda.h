@@ -163,6 +163,11 @@ uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent);
  * 16..22 = warp-specialised shapes with two 8-input tables per ring slot
  * (20: one table, same prefetching builders).  Returns the previous setting. */
 int par2cuda_set_comb_shape(int shape);
+/* Measures the rate (bytes/s) of one MD5 stream on one GPU thread with its
+ * data in registers (about 0.1 s): the dependency-chain ceiling of the
+ * one-stream-per-thread hash kernels (file MD5, IFSC, recovery-packet MD5).
+ * No counterpart in the reference. */
+int par2cuda_md5_chain_rate(double* bytes_per_s, void* stream);
 /* The comb CTA shape the next multiply-accumulate with num_rec recovery rows
  * will use (the set_comb_shape setting, else the automatic choice). */
 int par2cuda_comb_shape_for(unsigned num_rec);

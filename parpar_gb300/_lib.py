@@ -81,6 +81,7 @@ SIGNATURES = [
     ("par2cuda_device_error", _i, []),
     ("par2cuda_lop3_rate", _i, [ctypes.POINTER(ctypes.c_double), _vp]),
     ("par2cuda_comb_shape_for", _i, [_u]),
+    ("par2cuda_md5_chain_rate", _i, [ctypes.POINTER(ctypes.c_double), _vp]),
     ("par2cuda_muladd_scratch_bytes", _sz, [_u, _u]),
     ("par2cuda_muladd", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _i, _vp, _sz, _vp]),
     ("par2cuda_muladd_noalloc", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _vp]),

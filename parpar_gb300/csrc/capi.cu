@@ -129,6 +129,11 @@ int par2cuda_set_comb_shape(int shape) {
 	return p2c::set_comb_shape(shape);
 }
 
+int par2cuda_md5_chain_rate(double* bytes_per_s, void* stream) {
+	if(!bytes_per_s) { p2c::set_error("md5_chain_rate: null output"); return -1; }
+	return p2c::md5_chain_rate(bytes_per_s, (cudaStream_t)stream);
+}
+
 int par2cuda_comb_shape_for(unsigned num_rec) { return p2c::comb_shape_for(num_rec); }
 
 int par2cuda_lop3_rate(double* ops_per_s, void* stream) {

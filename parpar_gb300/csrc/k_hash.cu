@@ -220,6 +220,56 @@ int slice_hash(const void* rows, size_t pitchBytes, unsigned n, const uint32_t* 
 	return 0;
 }
 
+// ---- calibration: the MD5 dependency-chain bound ------------------------------
+// One MD5 stream on one GPU thread is bound by the latency of its serial
+// step chain (4 dependent integer ops per step), not by memory.  This kernel
+// runs that chain on register-resident data, one warp on one SM: the bytes/s
+// of one lane is the ceiling for the per-file and per-slice hash kernels.  The
+// message words depend on the block counter only, so, as with words loaded
+// ahead from memory, they stay off the chain; the chain itself carries across
+// blocks, so nothing can be hoisted.
+__global__ void __launch_bounds__(32) k_md5_chain(uint32_t* sink, unsigned blocks) {
+	uint32_t st[4] = {0x67452301u ^ threadIdx.x, 0xefcdab89u, 0x98badcfeu, 0x10325476u};
+	uint32_t base[16];
+#pragma unroll
+	for(int q = 0; q < 16; q++) base[q] = (uint32_t)(q + 1) * 0x9E3779B9u ^ threadIdx.x;
+	for(unsigned b = 0; b < blocks; b++) {
+		uint32_t m[16];
+#pragma unroll
+		for(int q = 0; q < 16; q++) m[q] = base[q] + b;
+		md5_block(st, m);
+	}
+	if((st[0] ^ st[1] ^ st[2] ^ st[3]) == 0x5EEDF00Du && blocks == 0) sink[threadIdx.x] = st[0];
+}
+
+int md5_chain_rate(double* bytesPerSec, cudaStream_t st) {
+	const unsigned blocks = 40000;   // ~25 ms at ~100 MB/s
+	cudaEvent_t e0, e1;
+	P2C_CUDA_TRY(cudaEventCreate(&e0));
+	P2C_CUDA_TRY(cudaEventCreate(&e1));
+	k_md5_chain<<<1, 32, 0, st>>>(nullptr, blocks / 8); // warm-up
+	float best = 0.f;
+	for(int rep = 0; rep < 3; rep++) {
+		cudaEventRecord(e0, st);
+		k_md5_chain<<<1, 32, 0, st>>>(nullptr, blocks);
+		cudaEventRecord(e1, st);
+		cudaError_t e = cudaEventSynchronize(e1);
+		if(e != cudaSuccess) {
+			cudaEventDestroy(e0); cudaEventDestroy(e1);
+			set_error("md5 chain calibration: %s", cudaGetErrorString(e));
+			return -1;
+		}
+		float ms = 0.f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if(rep == 0 || ms < best) best = ms;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	P2C_CUDA_TRY(cudaGetLastError());
+	*bytesPerSec = best > 0.f ? 64.0 * blocks / (best * 1e-3) : 0.0;
+	return 0;
+}
+
 // ---- per-file MD5 -----------------------------------------------------------
 // file f = rows first[f] .. first[f]+ceil(len[f]/sliceBytes)-1, each row
 // contributing sliceBytes bytes except the last.  One thread per file.

@@ -52,6 +52,8 @@ int comb_shape_for(unsigned R);  // the shape the next comb call with R rows use
 int comb_error_take();
 // measured three-input LOP3 throughput of the current device (ops/s)
 int lop3_rate(double* opsPerSec, cudaStream_t st);
+// one MD5 stream on one thread, data in registers: bytes/s
+int md5_chain_rate(double* bytesPerSec, cudaStream_t st);
 
 // bit-sliced LOP3 kernel and split-nibble table kernel (same contract, coefficient matrix [R][nIn])
 int xor_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,

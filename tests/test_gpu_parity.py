@@ -366,3 +366,14 @@ def test_muladd_index_matches_oracle():
     assert L.par2cuda_device_error() == 0
     # pitch below roundup(n_words, 64) is rejected
     assert L.par2cuda_muladd_index(d_in.data_ptr(), 32, n, d_idx.data_ptr(), d_rec.data_ptr(), pw, R, nw, 0, None) < 0
+
+
+def test_md5_chain_rate_calibration():
+    """The hash kernels' latency bound: one MD5 chain on one thread runs at
+    tens to hundreds of MB/s."""
+    pytest.importorskip("torch")
+    import ctypes
+    L = _lib.load()
+    v = ctypes.c_double(0)
+    _lib.check(L.par2cuda_md5_chain_rate(ctypes.byref(v), None), "md5_chain_rate")
+    assert 20e6 < v.value < 2e9, v.value
