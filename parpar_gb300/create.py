@@ -1,0 +1,258 @@
+"""PAR2 create from files on disk through the GPU backend: ParPar's PAR2Gen
+flow with its default output options, files in, finished .par2 files out.
+
+    create(["a.bin", "b.bin"], slice_size=1 << 20, recovery_slices=100, out_base="set")
+      -> ["set.par2", "set.vol00+01.par2", "set.vol01+02.par2", ...]
+
+Stages:
+  1. ingest: a reader thread reads every file sequentially, slice by slice, into
+     a ring of pinned host buffers; each filled buffer is copied to its rows of
+     the resident job (one 2-D host-to-device copy per buffer), overlapping
+     the next reads (the role of lib/fileseqreader.js feeding PAR2Gen);
+  2. on the device: MD5 of each file's first 16 KiB (file IDs), then, with the
+     input slices numbered in file-ID order, zero padding + checksum, the
+     recovery contraction, verification, IFSC entries and file MD5s
+     (ResidentJob.run) and the recovery-packet MD5s;
+  3. packets (parpar_gb300/par2packets.py) laid out into files as PAR2Gen does
+     by default.
+
+Restated from the reference (lib/par2gen.js, lib/par2.js):
+  display names, 'common' format .......... par2gen.js:727-756
+  input slice numbering by sorted file ID . par2.js:403-425
+  critical packet list and order .......... par2gen.js:770-781, 1026-1041
+  index file + pow2 recovery volumes ...... par2gen.js:783-803, 918-979
+  critical packet repetition (log 2) ...... par2gen.js:924-946, 104-128
+  volume names (alternative scheme) ....... par2gen.js:1501-1519
+The creator text is this backend's own unless one is passed.  The whole input
+must fit the device memory budget (no multi-pass chunking here).
+"""
+from __future__ import annotations
+
+import math
+import os
+import queue
+import threading
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import par2packets as P
+from .job import ResidentJob
+
+DEFAULT_CREATOR = "par2cuda (GB300 PAR2 recovery backend)"
+
+
+def js_round(x: float) -> int:
+    """JavaScript Math.round for non-negative values (halves round up)."""
+    return int(math.floor(x + 0.5))
+
+
+def display_names(paths):
+    """ParPar's default 'common' display names: each path relative to the
+    deepest directory containing all files, '/' separated (par2gen.js:727-756)."""
+    full = [os.path.abspath(p) for p in paths]
+    common = None
+    for f in full:
+        d = os.path.dirname(os.path.normpath(f)).split(os.sep)
+        if common is None:
+            common = d
+        else:
+            i = 0
+            while i < len(common) and i < len(d) and d[i] == common[i]:
+                i += 1
+            common = common[:i]
+    if not common:
+        return [os.path.basename(p) for p in paths]
+    if common[-1] == "":
+        common = common[:-1]
+    strip = len(os.sep.join(common)) + 1
+    return [f[strip:].replace(os.sep, "/") for f in full]
+
+
+def volume_name(num_slices: int, slice_offset: int, total_slices: int) -> str:
+    """'.volOFFSET+COUNT.par2' (par2gen.js:1501-1519, alternative scheme)."""
+    if not num_slices:
+        return ".par2"
+    digits = max(2, len(str(total_slices)))
+    return ".vol%s+%s.par2" % (str(slice_offset).zfill(digits), str(num_slices).zfill(digits))
+
+
+def pow2_volumes(recovery_slices: int, first_slices: int = 1, max_slices: int = 65535):
+    """(slices, first exponent) of every recovery volume: sizes 1, 2, 4, ... up
+    to max_slices, the last one holding the rest (par2gen.js:786-799)."""
+    out, i, n = [], 0, first_slices or 1
+    while i < recovery_slices:
+        f = min(n, recovery_slices - i)
+        out.append((f, i))
+        i += n
+        n = min(n * 2, max_slices)
+    return out
+
+
+@dataclass
+class OutFile:
+    name: str
+    packets: list          # ("crit", k) | ("recovery", exponent) | ("creator", None)
+
+
+def plan_files(out_base: str, n_crit: int, recovery_slices: int, index: bool = True, min_crit: int = 1,
+               max_crit: int = 0, first_slices: int = 1, max_slices: int = 65535):
+    """Output files and their packet order for ParPar's default options: an
+    index file, then pow2 recovery volumes; in a volume of n recovery slices
+    the critical packets are repeated max(round(log2 n), min_crit) times,
+    spread evenly after the recovery packets, creator last (par2gen.js:918-979)."""
+    files = []
+
+    def push(num_slices, offset):
+        if num_slices:
+            copies = max(js_round(math.log(num_slices) / math.log(2)), min_crit)
+            if max_crit:
+                copies = min(copies, max_crit)
+            crit_num = copies * n_crit
+            ratio = crit_num / num_slices
+            pk, written = [], 0
+            for i in range(num_slices):
+                pk.append(("recovery", i + offset))
+                while written < js_round(ratio * (i + 1)):
+                    pk.append(("crit", written % n_crit))
+                    written += 1
+        else:
+            pk = [("crit", j) for _ in range(min_crit) for j in range(n_crit)]
+        pk.append(("creator", None))
+        files.append(OutFile(out_base + volume_name(num_slices, offset, recovery_slices), pk))
+
+    if index:
+        push(0, 0)
+    for n, off in pow2_volumes(recovery_slices, first_slices, max_slices):
+        push(n, off)
+    if not files:
+        raise ValueError("nothing to generate: need an index or at least one recovery slice")
+    if len(files) == 1:
+        files[0].name = out_base + ".par2"
+    return files
+
+
+def _ingest(paths, sizes, job: ResidentJob, buf_rows: int = 32, nbuf: int = 3):
+    """Reads the files into the job's rows through a ring of pinned buffers
+    (reader thread) with one host-to-device copy per filled buffer."""
+    S = job.S
+    bufs = [torch.empty((buf_rows, S), dtype=torch.uint8, pin_memory=True) for _ in range(nbuf)]
+    free = [torch.cuda.Event() for _ in range(nbuf)]
+    for e in free:
+        e.record()
+    filled: queue.Queue = queue.Queue(maxsize=nbuf)
+    err = []
+
+    def reader():
+        try:
+            slot, k, r0, row = 0, 0, 0, 0
+            for path, size in zip(paths, sizes):
+                n = (size + S - 1) // S
+                with open(path, "rb", buffering=0) as f:
+                    for j in range(max(n, 1)):
+                        if k == 0:
+                            free[slot].synchronize()
+                            mv = memoryview(bufs[slot].numpy()).cast("B")
+                            r0 = row
+                        want = min(S, size - j * S) if size else 0
+                        got = 0
+                        while got < want:
+                            m = f.readinto(mv[k * S + got: k * S + want])
+                            if not m:
+                                raise IOError("%s: file shorter than its size" % path)
+                            got += m
+                        k += 1
+                        row += 1
+                        if k == buf_rows:
+                            filled.put((slot, r0, k))
+                            slot, k = (slot + 1) % nbuf, 0
+            if k:
+                filled.put((slot, r0, k))
+        except Exception as e:   # reported on the main thread
+            err.append(e)
+        filled.put(None)
+
+    th = threading.Thread(target=reader, daemon=True)
+    th.start()
+    dst = job.d_in.view(torch.uint8)
+    while True:
+        item = filled.get()
+        if item is None:
+            break
+        slot, r0, k = item
+        dst[r0:r0 + k, :S].copy_(bufs[slot][:k], non_blocking=True)
+        free[slot].record()
+    th.join()
+    if err:
+        raise err[0]
+    torch.cuda.current_stream().synchronize()
+
+
+def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator: str = DEFAULT_CREATOR,
+           names=None, device: int = 0, index: bool = True):
+    """Creates the PAR2 set for `paths`; returns the written file names."""
+    if slice_size <= 0 or slice_size % 4:
+        raise ValueError("slice size must be a positive multiple of 4")
+    if not (0 <= recovery_slices <= 65535):
+        raise ValueError("recovery slice count must be 0..65535")
+    paths = list(paths)
+    sizes = [os.path.getsize(p) for p in paths]
+    names = list(names) if names is not None else display_names(paths)
+    S = int(slice_size)
+    n_in = sum((s + S - 1) // S for s in sizes)
+    if n_in > 32768:
+        raise ValueError("PAR2 allows at most 32768 input slices (%d needed)" % n_in)
+    torch.cuda.set_device(device)
+    R = max(recovery_slices, 1)
+    job = ResidentJob(S, sizes, list(range(R)), device=device)
+    _ingest(paths, sizes, job)
+
+    # file IDs from the first 16 KiB, files sorted by ID, slices numbered in that order
+    m16 = job.md5_16k()
+    ids = [P.file_id(m16[f], sizes[f], names[f]) for f in range(len(paths))]
+    order = sorted(range(len(paths)), key=lambda f: int.from_bytes(ids[f], "little"))
+    nums = np.zeros(job.N, dtype=np.int64)
+    off = 0
+    for f in order:
+        n = (sizes[f] + S - 1) // S
+        first = int(job.first_row[f])
+        nums[first:first + n] = np.arange(off, off + n)
+        off += n
+    job.set_input_nums(nums)
+    job.run(hashes=True)
+    torch.cuda.synchronize()
+    if not bool(job.d_flags.all()):
+        raise RuntimeError("recovery checksum verification failed")
+
+    ifsc = job.d_ifsc.cpu().numpy().reshape(job.N, 20)
+    fmd5 = job.d_fmd5.cpu().numpy().reshape(len(paths), 16)
+    main, set_id = P.main_packet(S, ids)
+    crit = []
+    for f in order:
+        crit.append(P.filedesc_packets(set_id, ids[f], fmd5[f].tobytes(), m16[f], sizes[f], names[f]))
+        if sizes[f]:
+            first = int(job.first_row[f])
+            n = (sizes[f] + S - 1) // S
+            crit.append(P.ifsc_packet(set_id, ids[f], ifsc[first:first + n].tobytes()))
+    crit.append(main)
+    creator_pkt = P.creator_packet(set_id, creator)
+
+    plan = plan_files(out_base, len(crit), recovery_slices, index=index)
+    rec_md5 = job.recovery_packet_md5s(set_id) if recovery_slices else []
+    rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
+    rec_host.copy_(job.d_rec.view(torch.uint8)[:, :S])
+    rec_np = rec_host.numpy()
+    written = []
+    for of in plan:
+        with open(of.name, "wb") as fh:
+            for kind, k in of.packets:
+                if kind == "crit":
+                    fh.write(crit[k])
+                elif kind == "creator":
+                    fh.write(creator_pkt)
+                else:
+                    fh.write(P.recovery_packet(set_id, k, rec_np[k].tobytes(), rec_md5[k]))
+        written.append(of.name)
+    return written

@@ -122,6 +122,13 @@ class ResidentJob:
         self.sb = stream_b or torch.cuda.Stream(device=dev, priority=-10)
         self.launches_per_run = 8
 
+    def set_input_nums(self, input_nums):
+        """PAR2 input number of every row (e.g. once the file order by file ID
+        is known); the coefficients follow from them and the exponents."""
+        self.input_nums = np.asarray(input_nums)
+        coeff = par2_coefficients(self.input_nums, self.exps)
+        self.d_coeff = torch.from_numpy(coeff.view(np.int16)).to(self.dev)
+
     # -------------------------------------------------------------- inputs
     def fill_synthetic(self, seed: int):
         """Seeded rows (parpar_gb300.synth layout); bytes past each row's length are
