@@ -52,6 +52,10 @@ WORKLOADS = {
                        desc="512 input slices x 512 KiB, 200 recovery, GF contraction only (ncu capture size, 72-row CTAs)"),
     "profile_hash": dict(S=1048576, N=256, files=4, R=8, hashes=True,
                          desc="256 input slices x 1 MiB over 4 files, 8 recovery, with hashing (ncu capture size)"),
+    # configs[1] as files on the host's disk: files in, finished .par2 files out
+    "create": dict(S=2 * 1048576, N=2000, files=40, R=200, hashes=True,
+                   desc="the bandwidth workload's 40 files (3.9 GiB) written to the host's disk, then PAR2 create "
+                        "end to end: read, GPU hashing + recovery, .par2 index + pow2 volumes written"),
     # configs[4]: Poisson requests, admitted by free HBM, continuous batching
     "serving": dict(S=0, N=0, files=0, R=0, hashes=False, jobs=48,
                     desc="Poisson requests (sizes as the 64-job mix) at 200/s and at a sub-saturation rate; admission by "
@@ -606,6 +610,60 @@ def small_mix_run(args):
             "speedup_vs_per_job_launch": t_job / (ms / 1e3), "batched_mode": runner.mode, "mode_pass0_ms": modes}
 
 
+def run_create_workload(args, cfg):
+    """Files on disk -> .par2 files through parpar_gb300.create (wall clock;
+    the input files are written once before timing and are in the page cache)."""
+    import tempfile
+    import torch
+    from parpar_gb300 import synth
+    from parpar_gb300.create import create
+    S, N, R = cfg["S"], cfg["N"], cfg["R"]
+    file_lens = file_lengths(N, cfg["files"], S, seed=2000)
+    work = tempfile.mkdtemp(prefix="par2cuda_create_")
+    paths = []
+    row = 0
+    for f, ln in enumerate(file_lens):
+        n = (ln + S - 1) // S
+        data = synth.slices(1, row, n, S).reshape(-1)[:ln]
+        p = os.path.join(work, "file%02d.bin" % f)
+        data.tofile(p)
+        paths.append(p)
+        row += n
+    out_base = os.path.join(work, "set")
+    torch.cuda.set_device(0)
+    for _ in range(max(1, args.warmup)):
+        create(paths, S, R, out_base)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        outs = create(paths, S, R, out_base)
+        times.append(time.perf_counter() - t0)
+    out_bytes = sum(os.path.getsize(o) for o in outs)
+    for p in paths + outs:
+        os.remove(p)
+    os.rmdir(work)
+    t = float(np.median(times))
+    mul_adds = N * R * (S // 2)
+    line = {
+        "metric": METRIC, "value": mul_adds / t, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u16 GF(2^16)", "data": "synthetic seeded files on the host's disk (page cache)",
+        "config": {"workload": "create", "desc": cfg["desc"], "slice_bytes": S, "inputs": N, "recovery": R,
+                   "files": len(file_lens), "input_bytes": int(sum(file_lens)), "output_bytes": out_bytes,
+                   "output_files": len(outs)},
+        "input_GBps": sum(file_lens) / t / 1e9,
+        "e2e": {"value": mul_adds / t, "unit": UNIT, "h2d_bytes_per_step": int(sum(file_lens)),
+                "d2h_bytes_per_step": R * S, "path": "parpar_gb300.create: files -> pinned ring -> HBM -> "
+                                                     "hashes + recovery -> .par2 files (host wall clock)"},
+        "gpu_launches": None,
+    }
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1, window=args.cpu_window)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "method")}
+    print(json.dumps(line))
+    return 0
+
+
 def run_batched_workload(args, cfg):
     """configs[3]: the uneven 64-job mix, batched (graph replay) vs per-job launches."""
     import torch
@@ -693,6 +751,8 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the %s workload is reported against this backend's per-job path" % args.workload}))
             return 0
         return run_batched_workload(args, cfg) if args.workload == "batched" else run_serving_workload(args, cfg)
+    if args.workload == "create" and args.impl != "reference":
+        return run_create_workload(args, cfg)
     file_lens = file_lengths(cfg["N"], cfg["files"], cfg["S"], seed=2000)
     if args.impl == "reference":
         return run_reference(args, cfg, file_lens)

@@ -5,10 +5,11 @@ flow with its default output options, files in, finished .par2 files out.
       -> ["set.par2", "set.vol00+01.par2", "set.vol01+02.par2", ...]
 
 Stages:
-  1. ingest: a reader thread reads every file sequentially, slice by slice, into
-     a ring of pinned host buffers; each filled buffer is copied to its rows of
-     the resident job (one 2-D host-to-device copy per buffer), overlapping
-     the next reads (the role of lib/fileseqreader.js feeding PAR2Gen);
+  1. ingest: a reader thread reads the files (largest first), slice by slice,
+     into a ring of pinned host buffers; each filled buffer is copied to its
+     rows of the resident job (2-D host-to-device copies), overlapping the next
+     reads (the role of lib/fileseqreader.js feeding PAR2Gen), and each file's
+     MD5 starts on a high-priority stream as soon as its last row is copied;
   2. on the device: MD5 of each file's first 16 KiB (file IDs), then, with the
      input slices numbered in file-ID order, zero padding + checksum, the
      recovery contraction, verification, IFSC entries and file MD5s
@@ -134,9 +135,11 @@ def plan_files(out_base: str, n_crit: int, recovery_slices: int, index: bool = T
     return files
 
 
-def _ingest(paths, sizes, job: ResidentJob, buf_rows: int = 32, nbuf: int = 3):
-    """Reads the files into the job's rows through a ring of pinned buffers
-    (reader thread) with one host-to-device copy per filled buffer."""
+def _ingest(paths, sizes, job: ResidentJob, order, on_file=None, buf_rows: int = 32, nbuf: int = 3):
+    """Reads the files (in `order`) into their rows of the job through a ring
+    of pinned buffers (reader thread), one host-to-device copy per filled
+    buffer; on_file(f) runs on the calling thread once the copy holding file
+    f's last row has been issued."""
     S = job.S
     bufs = [torch.empty((buf_rows, S), dtype=torch.uint8, pin_memory=True) for _ in range(nbuf)]
     free = [torch.cuda.Event() for _ in range(nbuf)]
@@ -147,29 +150,33 @@ def _ingest(paths, sizes, job: ResidentJob, buf_rows: int = 32, nbuf: int = 3):
 
     def reader():
         try:
-            slot, k, r0, row = 0, 0, 0, 0
-            for path, size in zip(paths, sizes):
+            slot, k = 0, 0
+            rows, done = [], []          # destination row of each buffered slice, files completed
+            for f in order:
+                path, size = paths[f], sizes[f]
                 n = (size + S - 1) // S
-                with open(path, "rb", buffering=0) as f:
+                first = int(job.first_row[f])
+                with open(path, "rb", buffering=0) as fh:
                     for j in range(max(n, 1)):
                         if k == 0:
                             free[slot].synchronize()
                             mv = memoryview(bufs[slot].numpy()).cast("B")
-                            r0 = row
                         want = min(S, size - j * S) if size else 0
                         got = 0
                         while got < want:
-                            m = f.readinto(mv[k * S + got: k * S + want])
+                            m = fh.readinto(mv[k * S + got: k * S + want])
                             if not m:
                                 raise IOError("%s: file shorter than its size" % path)
                             got += m
+                        rows.append(first + j)
                         k += 1
-                        row += 1
+                        if j == max(n, 1) - 1:
+                            done.append(f)
                         if k == buf_rows:
-                            filled.put((slot, r0, k))
-                            slot, k = (slot + 1) % nbuf, 0
+                            filled.put((slot, rows, done))
+                            slot, k, rows, done = (slot + 1) % nbuf, 0, [], []
             if k:
-                filled.put((slot, r0, k))
+                filled.put((slot, rows, done))
         except Exception as e:   # reported on the main thread
             err.append(e)
         filled.put(None)
@@ -181,18 +188,36 @@ def _ingest(paths, sizes, job: ResidentJob, buf_rows: int = 32, nbuf: int = 3):
         item = filled.get()
         if item is None:
             break
-        slot, r0, k = item
-        dst[r0:r0 + k, :S].copy_(bufs[slot][:k], non_blocking=True)
+        slot, rows, done = item
+        # runs of consecutive destination rows -> one 2-D copy each
+        a = 0
+        while a < len(rows):
+            b = a + 1
+            while b < len(rows) and rows[b] == rows[b - 1] + 1:
+                b += 1
+            dst[rows[a]:rows[a] + (b - a), :S].copy_(bufs[slot][a:b], non_blocking=True)
+            a = b
         free[slot].record()
+        if on_file and done:
+            on_file(done)
     th.join()
     if err:
         raise err[0]
-    torch.cuda.current_stream().synchronize()
 
 
 def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator: str = DEFAULT_CREATOR,
-           names=None, device: int = 0, index: bool = True):
-    """Creates the PAR2 set for `paths`; returns the written file names."""
+           names=None, device: int = 0, index: bool = True, stats: dict | None = None):
+    """Creates the PAR2 set for `paths`; returns the written file names.
+    `stats`, if given, receives the wall-clock time (s) at which each stage
+    ended, measured from the call (stages are synchronised to measure them)."""
+    import time
+    t0 = time.perf_counter()
+
+    def mark(name, sync=None):
+        if stats is not None:
+            if sync is not None:
+                sync.synchronize()
+            stats[name] = time.perf_counter() - t0
     if slice_size <= 0 or slice_size % 4:
         raise ValueError("slice size must be a positive multiple of 4")
     if not (0 <= recovery_slices <= 65535):
@@ -207,10 +232,24 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
     torch.cuda.set_device(device)
     R = max(recovery_slices, 1)
     job = ResidentJob(S, sizes, list(range(R)), device=device)
-    _ingest(paths, sizes, job)
+    # largest file first: its MD5 chain (the longest serial work) starts as
+    # soon as its rows are on the device, while the other files are read
+    read_order = sorted(range(len(paths)), key=lambda f: -sizes[f])
+    job.file_md5_prepare(read_order)
+    launched = [0, 0]                   # [files launched, files complete]
+
+    def on_file(done):                  # file MD5s in launches of >= 5 files
+        launched[1] += len(done)
+        if launched[1] - launched[0] >= 5:
+            job.file_md5_launch(launched[0], launched[1])
+            launched[0] = launched[1]
+    _ingest(paths, sizes, job, read_order, on_file=on_file)
+    job.file_md5_launch(launched[0], len(paths))
+    mark("ingest", torch.cuda.current_stream())
 
     # file IDs from the first 16 KiB, files sorted by ID, slices numbered in that order
     m16 = job.md5_16k()
+    mark("md5_16k")
     ids = [P.file_id(m16[f], sizes[f], names[f]) for f in range(len(paths))]
     order = sorted(range(len(paths)), key=lambda f: int.from_bytes(ids[f], "little"))
     nums = np.zeros(job.N, dtype=np.int64)
@@ -221,8 +260,11 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
         nums[first:first + n] = np.arange(off, off + n)
         off += n
     job.set_input_nums(nums)
-    job.run(hashes=True)
+    job.run(hashes=True, file_md5=False)
+    mark("contraction+ifsc", job.sa)
+    job.file_md5_finish()
     torch.cuda.synchronize()
+    mark("file_md5")
     if not bool(job.d_flags.all()):
         raise RuntimeError("recovery checksum verification failed")
 
@@ -244,8 +286,9 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
     rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
     rec_host.copy_(job.d_rec.view(torch.uint8)[:, :S])
     rec_np = rec_host.numpy()
-    written = []
-    for of in plan:
+    def write(of):
+        # recovery packets: 68-byte header, then the slice straight from the
+        # pinned buffer (no per-packet copies)
         with open(of.name, "wb") as fh:
             for kind, k in of.packets:
                 if kind == "crit":
@@ -253,6 +296,12 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
                 elif kind == "creator":
                     fh.write(creator_pkt)
                 else:
-                    fh.write(P.recovery_packet(set_id, k, rec_np[k].tobytes(), rec_md5[k]))
-        written.append(of.name)
+                    fh.write(P.recovery_header(set_id, k, S, rec_md5[k]))
+                    fh.write(memoryview(rec_np[k]))
+        return of.name
+
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(8, len(plan))) as ex:
+        written = list(ex.map(write, plan))
+    mark("written")
     return written

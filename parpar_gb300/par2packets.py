@@ -86,6 +86,11 @@ def recovery_prefixes(set_id: bytes, exps) -> np.ndarray:
     return np.frombuffer(b"".join(head + struct.pack("<I", int(e)) for e in exps), dtype=np.uint8).reshape(len(exps), 36).copy()
 
 
+def recovery_header(set_id: bytes, exponent: int, data_len: int, md5: bytes) -> bytes:
+    """The 68 bytes of a RecvSlic packet before its data (`md5` from the GPU)."""
+    return MAGIC + struct.pack("<Q", 64 + 4 + data_len) + md5 + set_id + T_RECV + struct.pack("<I", exponent)
+
+
 def recovery_packet(set_id: bytes, exponent: int, data: bytes, md5: bytes | None = None) -> bytes:
     """RecvSlic packet; `md5` (from the GPU) must equal MD5(prefix || data)."""
     tail = set_id + T_RECV + struct.pack("<I", exponent) + data
