@@ -131,6 +131,12 @@ int par2cuda_end_input(par2cuda_ctx* ctx, par2cuda_done_fn cb, void* user);
 /* getOutput(index, output[, cb(valid)]) gf16/controller.h:185; `output`
  * holds >= current slice size bytes (src/gf.cc:668-669) */
 int par2cuda_get_output(par2cuda_ctx* ctx, unsigned index, void* output, par2cuda_done_fn cb, void* user);
+/* The `valid` of getOutput (gf16/controller.h:185, the bool its future
+ * resolves to) read synchronously: 1 = checksum valid, 0 = invalid, negative
+ * on error.  Waits for queued work (par2cuda_sync) and is meaningful once
+ * end_input has been issued; lets a caller copy outputs without a callback
+ * per slice. */
+int par2cuda_output_valid(par2cuda_ctx* ctx, unsigned index);
 /* discardOutput() gf16/controller.h:186-188: next batch overwrites */
 int par2cuda_discard_output(par2cuda_ctx* ctx);
 /* _hasAdded() gf16/controller.h:189-191 */

@@ -68,6 +68,7 @@ SIGNATURES = [
     ("par2cuda_flush", _i, [_vp]),
     ("par2cuda_end_input", _i, [_vp, DONE_FN, _vp]),
     ("par2cuda_get_output", _i, [_vp, _u, _vp, DONE_FN, _vp]),
+    ("par2cuda_output_valid", _i, [_vp, _u]),
     ("par2cuda_discard_output", _i, [_vp]),
     ("par2cuda_has_added", _i, [_vp]),
     ("par2cuda_is_empty", _i, [_vp]),

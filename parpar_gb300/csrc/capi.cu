@@ -84,6 +84,7 @@ int par2cuda_get_output(par2cuda_ctx* ctx, unsigned index, void* output, par2cud
 	if(!output) { p2c::set_error("null output buffer"); return -1; }
 	return ctx->eng->get_output(index, output, cb, user);
 }
+int par2cuda_output_valid(par2cuda_ctx* ctx, unsigned index) { P2C_CTX_CHECK(ctx); return ctx->eng->output_valid(index); }
 int par2cuda_discard_output(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); ctx->eng->discard_output(); return 0; }
 int par2cuda_has_added(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->has_added() ? 1 : 0; }
 int par2cuda_is_empty(par2cuda_ctx* ctx) { P2C_CTX_CHECK(ctx); return ctx->eng->is_empty() ? 1 : 0; }

@@ -316,6 +316,13 @@ int Engine::get_output(unsigned index, void* out, par2cuda_done_fn cb, void* use
 	return 0;
 }
 
+int Engine::output_valid(unsigned index) {
+	if(index >= outputExponents.size()) { set_error("recovery index %u not valid", index); return -1; }
+	sync();
+	if(!processingAdd) return 1;   // nothing computed: zeros, valid
+	return hFlags ? (int)hFlags[index] : -1;
+}
+
 int Engine::sync() {
 	std::unique_lock<std::mutex> lk(qm);
 	idleCv.wait(lk, [&] { return tq.empty() && !transferBusy; });

@@ -68,6 +68,8 @@ public:
 	int flush();
 	int end_input(par2cuda_done_fn cb, void* user);
 	int get_output(unsigned index, void* out, par2cuda_done_fn cb, void* user);
+	// checksum verdict of output `index` once end_input has completed (after sync)
+	int output_valid(unsigned index);
 	void discard_output() { processingAdd = false; }
 	bool has_added() const { return processingAdd; }
 	bool is_empty() const { return stagingActiveCount.load() == 0; }

@@ -377,3 +377,27 @@ def test_md5_chain_rate_calibration():
     v = ctypes.c_double(0)
     _lib.check(L.par2cuda_md5_chain_rate(ctypes.byref(v), None), "md5_chain_rate")
     assert 20e6 < v.value < 2e9, v.value
+
+
+def test_output_valid_matches_get_output_verdicts():
+    """par2cuda_output_valid (synchronous verdict) agrees with the get_output
+    callbacks, after outputs fetched without callbacks, and against the oracle."""
+    n, S, R = 23, 3000, 7
+    x = synth.slices(77, 0, n, S)
+    g = GfProc(S, input_batchsize=8)
+    g.set_recovery_slices(list(range(R)))
+    L = _lib.load()
+    assert L.par2cuda_output_valid(g._ctx, R) < 0          # index out of range
+    for i in range(n):
+        g.add_sync(i, x[i]).wait()
+    g.end_sync()
+    out = np.zeros((R, S), np.uint8)
+    null_cb = _lib.DONE_FN()
+    for r in range(R):
+        _lib.check(L.par2cuda_get_output(g._ctx, r, out[r].ctypes.data_as(ctypes.c_void_p), null_cb, None), "get")
+    _lib.check(L.par2cuda_sync(g._ctx), "sync")
+    assert [L.par2cuda_output_valid(g._ctx, r) for r in range(R)] == [1] * R
+    assert np.array_equal(out, O.recover(x, np.full(n, S), np.arange(n), list(range(R))))
+    other = np.zeros(S, np.uint8)
+    assert g.get_sync(3, other) and np.array_equal(other, out[3])
+    g.close()
