@@ -133,6 +133,25 @@ def measured_peaks():
         return None
 
 
+# ---------------------------------------------------------------------------- ranks
+def reduce_max(v: float, world: int, device=None) -> float:
+    """Max of a per-rank value over all ranks (the slowest rank's time); the
+    process group's backend decides the device of the exchange tensor."""
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(units_per_rank: float, ms: float, world: int) -> float:
+    """Units all ranks processed (replicas: the same work on each rank, weak
+    scaling) per second of the slowest rank's time."""
+    return units_per_rank * world / (ms / 1e3)
+
+
 # ---------------------------------------------------------------------------- CPU
 def cpu_baseline_run(cfg, file_lens, threads, window=32768, seed=1):
     """The reference algorithm's CPU implementation on a bounded sample of the
@@ -241,11 +260,7 @@ def run_ours(args, cfg, file_lens):
             dist.barrier()
 
     def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(v, world, dev)
 
     S, N, R = cfg["S"], cfg["N"], cfg["R"]
     mul_adds = N * R * (S // 2)
@@ -330,7 +345,7 @@ def run_ours(args, cfg, file_lens):
     ms = max_over_ranks(ms)
     comb_ms = float(np.mean([k0.elapsed_time(k1) for k0, k1, _, _ in ev]))
     hash_ms = float(np.mean([h0.elapsed_time(h1) for _, _, h0, h1 in ev])) if cfg["hashes"] else 0.0
-    value = mul_adds * world / (ms / 1e3)
+    value = whole_job_value(mul_adds, ms, world)
 
     # e2e: pinned host inputs -> H2D -> job -> D2H of every result, via the C ABI
     e2e = None
