@@ -355,8 +355,7 @@ def run_ours(args, cfg, file_lens):
         rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
         torch.cuda.synchronize()
         for _ in range(max(1, args.warmup // 2)):
-            job.upload(host_in)
-            job.run(hashes=cfg["hashes"])
+            job.run_from_host(host_in, hashes=cfg["hashes"])
             job.download(rec_host)
         torch.cuda.synchronize()
         barrier()
@@ -364,8 +363,7 @@ def run_ours(args, cfg, file_lens):
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(args.steps):
-            job.upload(host_in)
-            job.run(hashes=cfg["hashes"])
+            job.run_from_host(host_in, hashes=cfg["hashes"])
             _, _, _, flags = job.download(rec_host)
         e1.record()
         torch.cuda.synchronize()
@@ -374,7 +372,8 @@ def run_ours(args, cfg, file_lens):
         assert int(flags.sum()) == R
         e2e = {"value": mul_adds * world / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": N * S,
                "d2h_bytes_per_step": job.d2h_bytes(), "ms_per_step": ems,
-               "path": "par2cuda C ABI: pinned host slices -> H2D -> job -> D2H recovery + IFSC + file MD5 + verdicts"}
+               "path": "par2cuda C ABI: pinned host slices -> H2D (per file, largest first, file MD5s starting as "
+                       "files land) -> job -> D2H recovery + IFSC + file MD5 + verdicts"}
     # e2e through the reference-facing plugin boundary: the PAR2ProcCUDA engine
     # driven like GfProc (src/gf.cc AddSlice / EndInput / GetOutputSlice) with
     # pinned host slices; GF + internal checksum only (the reference's plugin
@@ -759,6 +758,8 @@ def main():
                     help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline_gf.traffic")
     args = ap.parse_args()
     cfg = WORKLOADS[args.workload]
+    if args.workload in ("batched", "serving", "create") and int(os.environ.get("RANK", "0")) != 0:
+        return 0   # single-GPU workloads: under torchrun only rank 0 measures
     if args.workload in ("batched", "serving"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the %s workload is reported against this backend's per-job path" % args.workload}))

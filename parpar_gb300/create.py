@@ -229,7 +229,7 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
     n_in = sum((s + S - 1) // S for s in sizes)
     if n_in > 32768:
         raise ValueError("PAR2 allows at most 32768 input slices (%d needed)" % n_in)
-    torch.cuda.set_device(device)
+    torch.cuda.set_device(device)   # the job's streams and buffers live on this device
     R = max(recovery_slices, 1)
     job = ResidentJob(S, sizes, list(range(R)), device=device)
     # largest file first: its MD5 chain (the longest serial work) starts as

@@ -150,6 +150,9 @@ class ResidentJob:
         range of it.  Device arrays and streams are made here, before the
         rows are copied, so that a launch is a bare C-ABI call."""
         order = [int(f) for f in order]
+        if getattr(self, "_ro", None) == order:
+            self._md5_used = 0
+            return
         self._ro = order
         self._ro_flen = torch.tensor([self.file_lens[f] for f in order], dtype=torch.int64, device=self.dev)
         self._ro_first = torch.tensor([int(self.first_row[f]) for f in order], dtype=torch.int32, device=self.dev)
@@ -182,6 +185,31 @@ class ResidentJob:
         for st in self._md5_streams:
             cur.wait_stream(st)
         self.d_fmd5.view(-1, 16).index_copy_(0, self._ro_idx, self._ro_out.view(-1, 16)[: len(self._ro)])
+
+    def run_from_host(self, host_rows: torch.Tensor, hashes: bool = True, group: int = 5):
+        """upload() + run() with the copies and the file MD5s overlapped: files
+        are copied largest first, one 2-D copy per file, and the MD5 chains of
+        every `group` completed files start at once on their own streams
+        (the longest chain starts after the first file's copy instead of after
+        the whole upload).  host_rows: pinned [N, S] rows in row order."""
+        order = sorted(range(len(self.file_lens)), key=lambda f: -self.file_lens[f])
+        if hashes:
+            self.file_md5_prepare(order)
+        dst = self.d_in.view(torch.uint8)
+        done = launched = 0
+        for f in order:
+            a = int(self.first_row[f])
+            n = max(1, (self.file_lens[f] + self.S - 1) // self.S)
+            dst[a:a + n, : self.S].copy_(host_rows[a:a + n], non_blocking=True)
+            done += 1
+            if hashes and done - launched >= group:
+                self.file_md5_launch(launched, done)
+                launched = done
+        if hashes:
+            self.file_md5_launch(launched, done)
+        self.run(hashes=hashes, file_md5=False)
+        if hashes:
+            self.file_md5_finish()
 
     def run(self, hashes: bool = True, file_md5: bool = True):
         """Issues the whole job on streams A and B (asynchronous); file_md5 =

@@ -30,9 +30,17 @@ def test_resident_job_matches_oracle(S, file_lens, R):
             host[first[f] + k, :len(chunk)] = chunk
     exps = list(range(3, 3 + R))
     job = ResidentJob(S, file_lens, exps)
-    job.upload(torch.from_numpy(host).pin_memory())
-    for _ in range(2):  # a second run over the same rows gives the same results
-        job.run()
+    pinned = torch.from_numpy(host).pin_memory()
+    job.upload(pinned)
+    # twice through upload + run, then twice through run_from_host (per-file
+    # copies overlapped with the file MD5s, in launch groups of 2 files)
+    for it in range(4):
+        if it < 2:
+            job.run()
+        else:
+            job.d_in.zero_()
+            job.d_fmd5.zero_()
+            job.run_from_host(pinned, group=2)
         rec, ifsc, fmd5, flags = job.download()
         torch.cuda.synchronize()
         assert flags.numpy().tolist() == [1] * R

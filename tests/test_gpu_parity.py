@@ -401,3 +401,25 @@ def test_output_valid_matches_get_output_verdicts():
     other = np.zeros(S, np.uint8)
     assert g.get_sync(3, other) and np.array_equal(other, out[3])
     g.close()
+
+
+def test_max_recovery_count():
+    """32768 recovery slices (par-compare's large-recovery shape), exponents
+    spread up to 65534, a few small inputs."""
+    n, S = 3, 32
+    rng = np.random.default_rng(32768)
+    exps = sorted(rng.choice(65535, size=32768, replace=False).tolist())
+    x = synth.slices(9, 0, n, S)
+    out, valid = create_recovery(x, np.full(n, S), np.arange(n), exps)
+    assert valid.all()
+    assert np.array_equal(out, O.recover(x, np.full(n, S), np.arange(n), exps))
+
+
+def test_max_input_count():
+    """32768 inputs (input numbers 0..32767, the PAR2 maximum), short slices."""
+    n, S, R = 32768, 8, 3
+    x = synth.slices(11, 0, n, S)
+    exps = [0, 1, 65534]
+    out, valid = create_recovery(x, np.full(n, S), np.arange(n), exps, input_batchsize=4096)
+    assert valid.all()
+    assert np.array_equal(out, O.recover(x, np.full(n, S), np.arange(n), exps))
