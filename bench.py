@@ -52,15 +52,15 @@ WORKLOADS = {
                        desc="512 input slices x 512 KiB, 200 recovery, GF contraction only (ncu capture size, 72-row CTAs)"),
     "profile_hash": dict(S=1048576, N=256, files=4, R=8, hashes=True,
                          desc="256 input slices x 1 MiB over 4 files, 8 recovery, with hashing (ncu capture size)"),
-    # configs[1] as files on the host's disk: files in, finished .par2 files out
+    # the bandwidth workload as files on the host's disk: files in, finished .par2 files out
     "create": dict(S=2 * 1048576, N=2000, files=40, R=200, hashes=True,
                    desc="the bandwidth workload's 40 files (3.9 GiB) written to the host's disk, then PAR2 create "
                         "end to end: read, GPU hashing + recovery, .par2 index + pow2 volumes written"),
-    # configs[4]: Poisson requests, admitted by free HBM, continuous batching
+    # serving: Poisson requests, admitted by free HBM, continuous batching
     "serving": dict(S=0, N=0, files=0, R=0, hashes=False, jobs=48,
                     desc="Poisson requests (sizes as the 64-job mix) at 200/s and at a sub-saturation rate; admission by "
                          "free HBM (<=150 GB), chunked when over budget; jobs/s and p50/p99 latency"),
-    # configs[3]: 64 uneven jobs, one persistent graph-captured launch per pass
+    # batched: 64 uneven jobs, one graph-captured sequence of launches per pass
     "batched": dict(S=0, N=0, files=0, R=0, hashes=False, jobs=64,
                     desc="64 PAR2 jobs: N log-uniform [10,5000], S uniform 64 KiB..8 MiB (4-byte steps), R 1-30% of N; "
                          "byte-window passes under a 64 GiB HBM budget; persistent graph-captured comb launches vs per-job launches"),
@@ -558,7 +558,7 @@ def run_ours(args, cfg, file_lens):
 
 
 def run_serving_workload(args, cfg):
-    """configs[4]: Poisson arrivals at 200/s (offered load above the GPU's
+    """Serving: Poisson arrivals at 200/s (offered load above the GPU's
     capacity) and at a sub-saturation rate; latency = completion - arrival."""
     import torch
     from parpar_gb300 import autotune
@@ -677,7 +677,7 @@ def run_create_workload(args, cfg):
 
 
 def run_batched_workload(args, cfg):
-    """configs[3]: the uneven 64-job mix, batched (graph replay) vs per-job launches."""
+    """The uneven 64-job mix, batched (graph replay) vs per-job launches."""
     import torch
     from parpar_gb300 import autotune
     from parpar_gb300.batch import BatchRunner, make_job_mix

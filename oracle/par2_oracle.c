@@ -2,7 +2,7 @@
  * ORACLE — test infrastructure, not product code.
  *
  * A plain-C restatement of the reference's CPU algorithm for the PAR2 recovery
- * path (ParPar, Ravencentric/ParPar).  It is the checker for the CUDA path:
+ * path (ParPar, Ravencentric/ParPar).  The CUDA path is tested against it:
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
  * it.  The product library (libpar2cuda.so) never links or calls it.
  *

@@ -264,7 +264,8 @@ def _sampled_check(torch, d_in, pw, n, d_rec, R, S, exps, samples=48, seed=0):
 
 @pytest.mark.parametrize("n,R,S", [(4096, 4096, 262144 // 16), (2000, 200, 2 * 1048576 // 16)])
 def test_large_shapes_sampled(n, R, S):
-    """Config-3 and config-2 counts (inputs x recovery) at reduced slice size:
+    """The dense (4096 x 4096) and bandwidth (2000 x 200) workloads' counts
+    (inputs x recovery) at reduced slice size:
     every checksum verifies and sampled words match the oracle."""
     torch = pytest.importorskip("torch")
     L = _lib.load()

@@ -73,9 +73,9 @@ def test_small_inverse_agrees():
 
 @pytest.mark.parametrize("N,R,S,k,method", [
     (40, 12, 4100, 12, 1),
-    (2000, 200, 65536, 200, 1),     # config-2 counts, 64 KiB slices, every recovery slice used
+    (2000, 200, 65536, 200, 1),     # the bandwidth workload's counts, 64 KiB slices, every recovery slice used
     (300, 64, 32768, 50, 4),        # the tensor-core variant
-    (4096, 96, 16384, 96, 1),       # config-3 input count
+    (4096, 96, 16384, 96, 1),       # the dense workload's input count
 ])
 def test_encode_erase_decode(N, R, S, k, method):
     torch = pytest.importorskip("torch")
