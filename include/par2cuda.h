@@ -166,8 +166,10 @@ uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent);
  * autotuner's knob): 0 = chosen from the number of recovery rows, 1..9 = a
  * fixed (rows per warp x warps) shape; 10..15 = warp-specialised shapes
  * (4 table-building warps + 8 or 12 lookup warps, 2 or 4 words per lane);
- * 16..22 = warp-specialised shapes with two 8-input tables per ring slot
- * (20: one table, same prefetching builders).  Returns the previous setting. */
+ * 16..25 = warp-specialised shapes with two 8-input tables per ring slot
+ * (20: one table, same prefetching builders); 26..28 = the same with the
+ * builder warpgroup's registers moved to the lookup warps (84, 72 and 96
+ * rows).  Returns the previous setting. */
 int par2cuda_set_comb_shape(int shape);
 /* Measures the rate (bytes/s) of one MD5 stream on one GPU thread with its
  * data in registers (about 0.1 s): the dependency-chain ceiling of the

@@ -24,6 +24,8 @@ def comb_kernel_name(shape: int) -> str:
     """Kernel behind a comb CTA shape id (par2cuda_set_comb_shape)."""
     if 10 <= shape <= 15:
         return "k_comb_ws"
+    if shape >= 26:
+        return "k_comb_pair_rr"
     if shape >= 16:
         return "k_comb_pair"
     return "k_comb_muladd"

@@ -126,7 +126,7 @@ uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent) {
 }
 
 int par2cuda_set_comb_shape(int shape) {
-	if(shape < 0 || shape > 25) { p2c::set_error("comb shape %d out of range 0..25", shape); return -1; }
+	if(shape < 0 || shape > 28) { p2c::set_error("comb shape %d out of range 0..28", shape); return -1; }
 	return p2c::set_comb_shape(shape);
 }
 

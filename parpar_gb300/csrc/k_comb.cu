@@ -438,7 +438,7 @@ static int launch_comb_ws(const uint16_t* in, size_t inPitch, unsigned nIn, cons
 // its mbarrier phases running from unit to unit.  Returns false when a
 // bounded wait gave up (g_comb_error is set); the thread then does no more
 // work in this unit but still returns normally.
-template<int RPW, int NL, int GP>
+template<int RPW, int NL, int GP, int ROLE = 0>   // ROLE: 0 = by warp index, 1 = builder, 2 = lookup
 __device__ __forceinline__ bool pair_unit(
 	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
 	const uint4* __restrict__ idx, unsigned G,
@@ -457,7 +457,7 @@ __device__ __forceinline__ bool pair_unit(
 	const size_t colWord = tile * P2C_TILE_WORDS + lane * 2;
 	const unsigned NS = (G + GP - 1) / GP;             // ring slots of this unit
 
-	if(warp >= NL) {
+	if(ROLE != 2 && (ROLE == 1 || warp >= NL)) {
 		// ---------------- builders: 4 warps x 4 high nibbles of each table
 		const int bw = warp - NL;
 		const int bt = threadIdx.x - NL * 32; // 0..127
@@ -518,56 +518,60 @@ __device__ __forceinline__ bool pair_unit(
 		return true;
 	}
 
-	// ---------------- lookups
-	uint32_t acc[RPW][16];
+	if constexpr(ROLE == 1) {
+		return true;
+	} else {
+		// ---------------- lookups
+		uint32_t acc[RPW][16];
 #pragma unroll
-	for(int s = 0; s < RPW; s++)
+		for(int s = 0; s < RPW; s++)
 #pragma unroll
-		for(int k = 0; k < 16; k++) acc[s][k] = 0;
-	const uint32_t lwb = (uint32_t)lane * 4;
+			for(int k = 0; k < 16; k++) acc[s][k] = 0;
+		const uint32_t lwb = (uint32_t)lane * 4;
 
-	for(unsigned sl = 0; sl < NS; sl++) {
-		const unsigned gs = gs0 + sl;
-		const int b = gs & 1;
-		if(!mbar_wait(&bars[b], (gs >> 1) & 1)) return false;
-		const uint32_t lw = lwb + b * 128;
+		for(unsigned sl = 0; sl < NS; sl++) {
+			const unsigned gs = gs0 + sl;
+			const int b = gs & 1;
+			if(!mbar_wait(&bars[b], (gs >> 1) & 1)) return false;
+			const uint32_t lw = lwb + b * 128;
 #pragma unroll
-		for(int s = 0; s < RPW; s++) {
-			const int j = warp * RPW + s;
-			if(rbase + j < R) {
-				uint32_t qq[GP][4];
+			for(int s = 0; s < RPW; s++) {
+				const int j = warp * RPW + s;
+				if(rbase + j < R) {
+					uint32_t qq[GP][4];
 #pragma unroll
-				for(int t = 0; t < GP; t++) {
-					const uint4 q = idxs[(b * GP + t) * RT + j];
-					qq[t][0] = q.x; qq[t][1] = q.y; qq[t][2] = q.z; qq[t][3] = q.w;
-				}
+					for(int t = 0; t < GP; t++) {
+						const uint4 q = idxs[(b * GP + t) * RT + j];
+						qq[t][0] = q.x; qq[t][1] = q.y; qq[t][2] = q.z; qq[t][3] = q.w;
+					}
 #pragma unroll
-				for(int k = 0; k < 16; k++) {
-					// byte0 <- lw.byte0, byte1 <- q.byte(k&3), bytes 2,3 <- lw.byte1 (= 0)
-					const uint32_t sel = 4u | ((uint32_t)(k & 3) << 4) | (5u << 8) | (5u << 12);
-					uint32_t v = *reinterpret_cast<const uint32_t*>(tbl + __byte_perm(qq[0][k >> 2], lw, sel));
-					if(GP == 2) v ^= *reinterpret_cast<const uint32_t*>(tbl + TBL + __byte_perm(qq[GP - 1][k >> 2], lw, sel));
-					acc[s][k] ^= v;
+					for(int k = 0; k < 16; k++) {
+						// byte0 <- lw.byte0, byte1 <- q.byte(k&3), bytes 2,3 <- lw.byte1 (= 0)
+						const uint32_t sel = 4u | ((uint32_t)(k & 3) << 4) | (5u << 8) | (5u << 12);
+						uint32_t v = *reinterpret_cast<const uint32_t*>(tbl + __byte_perm(qq[0][k >> 2], lw, sel));
+						if(GP == 2) v ^= *reinterpret_cast<const uint32_t*>(tbl + TBL + __byte_perm(qq[GP - 1][k >> 2], lw, sel));
+						acc[s][k] ^= v;
+					}
 				}
 			}
+			__syncwarp();
+			if(lane == 0) mbar_arrive(&bars[2 + b]);
 		}
-		__syncwarp();
-		if(lane == 0) mbar_arrive(&bars[2 + b]);
-	}
 
 #pragma unroll
-	for(int s = 0; s < RPW; s++) {
-		const unsigned r = rbase + warp * RPW + s;
-		if(r < R) {
-			uint32_t v = acc[s][15];
+		for(int s = 0; s < RPW; s++) {
+			const unsigned r = rbase + warp * RPW + s;
+			if(r < R) {
+				uint32_t v = acc[s][15];
 #pragma unroll
-			for(int k = 14; k >= 0; k--) v = mul2x2(v) ^ acc[s][k];
-			uint32_t* p = reinterpret_cast<uint32_t*>(rec + (size_t)r * recPitch + colWord);
-			if(accumulate) v ^= *p;
-			*p = v;
+				for(int k = 14; k >= 0; k--) v = mul2x2(v) ^ acc[s][k];
+				uint32_t* p = reinterpret_cast<uint32_t*>(rec + (size_t)r * recPitch + colWord);
+				if(accumulate) v ^= *p;
+				*p = v;
+			}
 		}
+		return true;
 	}
-	return true;
 }
 
 template<int RPW, int NL, int GP>
@@ -597,6 +601,34 @@ __global__ void __launch_bounds__((NL + 4) * 32, 1) k_comb_pair(
 	const size_t tile = blockIdx.x / rblocks;
 	const unsigned rb = blockIdx.x - (unsigned)tile * rblocks;
 	pair_unit<RPW, NL, GP>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate, tile, rb * (RPW * NL), 0u, smem);
+}
+
+// Paired kernel with register reallocation: the builder warpgroup gives up
+// registers (setmaxnreg.dec to RB) and the lookup warpgroups take them
+// (setmaxnreg.inc to RL), so a lookup warp can hold more recovery rows' P
+// accumulators (more rows per CTA share each table build).  The two roles are
+// separate branches from the start, each with its own register limit.  The
+// host launches it only when the launch's register pool covers the split.
+template<int RPW, int NL, int GP, int RL, int RB>
+__global__ void __launch_bounds__((NL + 4) * 32, 1) k_comb_pair_rr(
+	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
+	const uint4* __restrict__ idx, unsigned G,
+	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, int accumulate)
+{
+	static_assert(NL % 4 == 0, "lookup warps form whole warpgroups");
+	extern __shared__ __align__(16) uint8_t smem[];
+	pair_init_bars<RPW, NL, GP>(smem);
+	__syncthreads();
+	const unsigned rblocks = (R + RPW * NL - 1) / (RPW * NL);
+	const size_t tile = blockIdx.x / rblocks;
+	const unsigned rb = blockIdx.x - (unsigned)tile * rblocks;
+	if((threadIdx.x >> 5) >= NL) {
+		asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" :: "n"(RB));
+		pair_unit<RPW, NL, GP, 1>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate, tile, rb * (RPW * NL), 0u, smem);
+	} else {
+		asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" :: "n"(RL));
+		pair_unit<RPW, NL, GP, 2>(in, inPitch, nIn, idx, G, rec, recPitch, R, accumulate, tile, rb * (RPW * NL), 0u, smem);
+	}
 }
 
 // Persistent batched form of the paired kernel: one CTA per SM takes (job,
@@ -846,6 +878,30 @@ static int launch_comb_pair(const uint16_t* in, size_t inPitch, unsigned nIn, co
 	return 0;
 }
 
+// Launches the register-reallocating kernel when the launch's register pool
+// (registers per thread at launch x threads) covers the split and the split
+// lowers the builders and raises the lookups; otherwise returns 1 and the
+// caller launches another shape.
+template<int RPW, int NL, int GP, int RL, int RB>
+static int launch_comb_pair_rr(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* idx, uint16_t* rec,
+                               size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st)
+{
+	constexpr int RT = RPW * NL;
+	constexpr int THREADS = (NL + 4) * 32;
+	cudaFuncAttributes fa;
+	P2C_CUDA_TRY(cudaFuncGetAttributes(&fa, k_comb_pair_rr<RPW, NL, GP, RL, RB>));
+	if(fa.numRegs < RB || fa.numRegs > RL || fa.numRegs * THREADS < RL * NL * 32 + RB * 128) return 1;
+	const size_t smem = 65536 * GP + 2 * GP * RT * sizeof(uint4) + 4 * sizeof(uint64_t);
+	P2C_CUDA_TRY(cudaFuncSetAttribute(k_comb_pair_rr<RPW, NL, GP, RL, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const unsigned G = (nIn + 7) / 8;
+	const unsigned long long ctas = (unsigned long long)((nWords + P2C_TILE_WORDS - 1) / P2C_TILE_WORDS) * ((R + RT - 1) / RT);
+	if(ctas > 0x7FFFFFFFull) { set_error("comb: %llu CTAs exceed the grid limit", ctas); return -1; }
+	k_comb_pair_rr<RPW, NL, GP, RL, RB><<<(unsigned)ctas, THREADS, smem, st>>>(in, inPitch, nIn, idx, G, rec, recPitch, R,
+	                                                                         accumulate);
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
 template<int RPW, int NL, int GP>
 static int launch_pair_batched(const BatchJob* jobs, unsigned nJobs, unsigned long long totalUnits,
                                unsigned long long* counter, cudaStream_t st)
@@ -877,16 +933,25 @@ int comb_error_take() {
 static std::atomic<int> g_comb_shape{0};
 int set_comb_shape(int shape) { return g_comb_shape.exchange(shape); }
 
-// Automatic CTA shape from R (measured on 2000 x 1 MiB and 4096 x 256 KiB
-// jobs): above 8 rows the paired-table kernel wins even with padded rows
-// (R = 16: 2.1 T vs 1.8 T word mul-adds/s for the best narrow shape), with
-// 72-row blocks (6 rows x 12 lookup warps) or 64-row blocks (8 x 8, 3 %
-// slower per row), whichever costs less after padding the last block.  Up to
-// 8 rows a single-warp one-phase CTA builds its own tables.
+// Automatic CTA shape from R (measured on 2000 x 1 MiB, 2000 x 2 MiB and
+// 4096 x 256 KiB jobs): above 8 rows the paired-table kernel wins even with
+// padded rows (R = 16: 2.1 T vs 1.8 T word mul-adds/s for the best narrow
+// shape).  Candidates, with their measured rate per row relative to the
+// 72-row block: 72 rows (6 rows x 12 lookup warps, 1.00), 64 rows (8 x 8,
+// 0.97) and 96 rows (8 x 12 with register reallocation, 1.018); the one with
+// the lowest padded-rows / rate wins above 72 rows.  Up to 8 rows a
+// single-warp one-phase CTA builds its own tables.
 int comb_auto_shape(unsigned R) {
 	if(R <= 8) return 1;
-	const unsigned r72 = (R + 71) / 72 * 72, r64 = (R + 63) / 64 * 64;
-	return (double)r72 <= (double)r64 / 0.97 ? 16 : 18;
+	if(R <= 72) return 16;   // one block either way: measured faster than 64-row blocks at R = 16, 32, 64
+	static const struct { int shape; unsigned rows; double rate; } cand[3] = {{16, 72, 1.0}, {18, 64, 0.97}, {28, 96, 1.018}};
+	int best = 16;
+	double bestCost = 1e300;
+	for(const auto& c : cand) {
+		const double cost = (double)((R + c.rows - 1) / c.rows * c.rows) / c.rate;
+		if(cost < bestCost) { bestCost = cost; best = c.shape; }
+	}
+	return best;
 }
 
 int comb_shape_for(unsigned R) {
@@ -931,6 +996,13 @@ int comb_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint4* i
 	case 23: return launch_comb_pair<8, 4, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 24: return launch_comb_pair<8, 2, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	case 25: return launch_comb_pair<8, 1, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	case 26: case 27: case 28: {
+		int rc = shape == 26 ? launch_comb_pair_rr<7, 12, 2, 144, 56>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st)
+		       : shape == 27 ? launch_comb_pair_rr<6, 12, 2, 152, 56>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st)
+		       : launch_comb_pair_rr<8, 12, 2, 152, 56>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+		if(rc != 1) return rc;
+		return launch_comb_pair<6, 12, 2>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
+	}
 	default: return launch_comb<8, 12>(in, inPitch, nIn, idx, rec, recPitch, R, nWords, accumulate, st);
 	}
 }

@@ -292,7 +292,7 @@ def test_large_shapes_sampled(n, R, S):
     _sampled_check(torch, d_in, pw, n, d_rec, R, S, exps)
 
 
-@pytest.mark.parametrize("shape", list(range(0, 26)))
+@pytest.mark.parametrize("shape", list(range(0, 29)))
 def test_comb_every_cta_shape(shape):
     """Every comb CTA shape (rows per warp x warps) gives the oracle's result,
     including partial recovery blocks and a ragged input group."""
