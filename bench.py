@@ -33,9 +33,12 @@ sys.path.insert(0, ROOT)
 METRIC = "GF16 mul-adds/s"
 UNIT = "mul-adds/s"
 
-# one ncu capture of k_comb_pair<6,12,2> (512 inputs x 200 recovery x 512 KiB):
+# one ncu capture per contraction kernel on a 512-input x 512 KiB case:
 # dram__bytes_read.sum + dram__bytes_write.sum, and the algorithmic (N + R) x S
-PAIR_TRAFFIC = (270406912 + 87077120, (512 + 200) * 524288)
+KERNEL_TRAFFIC = {
+    "k_comb_pair": (270406912 + 87077120, (512 + 200) * 524288, "k_comb_pair<6,12,2> on 512x200x512KiB"),
+    "k_comb_pair_rr": (268913408 + 81736448, (512 + 192) * 524288, "k_comb_pair_rr<8,12,2,152,56> on 512x192x512KiB"),
+}
 
 WORKLOADS = {
     # name: (slice bytes, input slices, files, recovery slices, hashing)
@@ -531,14 +534,14 @@ def run_ours(args, cfg, file_lens):
     }
     if args.traffic_bytes:
         line["roofline_gf"]["traffic"] = args.traffic_bytes
-    elif kname == "k_comb_pair":
+    elif kname in KERNEL_TRAFFIC:
         # DRAM bytes per launch scaled from the ncu capture of the same kernel
-        # on 512 x 200 x 512 KiB (profiles/comb_pair_512x200x512KiB.md):
-        # inputs are read once and recovery rows written once, so traffic grows
-        # with (N + R) x S
-        line["roofline_gf"]["traffic"] = PAIR_TRAFFIC[0] / PAIR_TRAFFIC[1] * alg_bytes
-        line["roofline_gf"]["traffic_source"] = "ncu dram__bytes_read+write of k_comb_pair<6,12,2> on 512x200x512KiB " \
-            "(%.1f MB for %.1f MB algorithmic), scaled by (N+R)*S" % (PAIR_TRAFFIC[0] / 1e6, PAIR_TRAFFIC[1] / 1e6)
+        # (profiles/): inputs are read once and recovery rows written once, so
+        # traffic grows with (N + R) x S
+        tb, ab, what = KERNEL_TRAFFIC[kname]
+        line["roofline_gf"]["traffic"] = tb / ab * alg_bytes
+        line["roofline_gf"]["traffic_source"] = "ncu dram__bytes_read+write of %s (%.1f MB for %.1f MB algorithmic), " \
+            "scaled by (N+R)*S" % (what, tb / 1e6, ab / 1e6)
     if cfg["hashes"]:
         big = max(file_lens)
         line["roofline_md5"] = {
