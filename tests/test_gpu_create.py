@@ -30,6 +30,10 @@ def _files(tmp_path, sizes, names, seed):
     (65536, 3, [65536 * 5 + 7, 20000], ["x", "y"]),
     (1024, 1, [16384 + 3000], ["only"]),
     (2048, 0, [5000, 9000], ["m", "n"]),
+    # par-compare's file sizes with its 65521*4-byte slices and 200 recovery slices
+    (65521 * 4, 200, [1, 8, 65521, 13631477], ["f1", "f8", "f65521", "f13631477"]),
+    # par-compare's 40000-byte slices with 10000 recovery slices (pow2 volumes up to 4096)
+    (40000, 10000, [400000], ["big.bin"]),
 ])
 def test_create_par2_files(tmp_path, S, R, sizes, names):
     pytest.importorskip("torch")
@@ -53,7 +57,7 @@ def test_create_par2_files(tmp_path, S, R, sizes, names):
             rows.append(np.frombuffer(chunk + bytes(S - len(chunk)), dtype=np.uint8))
             lens.append(len(chunk))
     x = np.stack(rows)
-    rec = O.recover(x, np.array(lens), np.arange(len(rows)), list(range(R))) if R else None
+    rec = O.recover(x, np.array(lens), np.arange(len(rows)), list(range(R)), threads=8) if R else None
 
     n_crit = sum(1 + (1 if sizes[i] else 0) for i in range(len(paths))) + 1
     plan = plan_files(str(tmp_path / "set"), n_crit, R)
