@@ -386,7 +386,7 @@ def run_ours(args, cfg, file_lens):
         from parpar_gb300.gfproc import GfProc
         from parpar_gb300.job import file_layout
         _, row_lens = file_layout(file_lens, S)
-        g = GfProc(S, method=args.method)
+        g = GfProc(S, method=args.method, device=local)
         g.set_recovery_slices(list(range(R)))
         views = [host_in[i, : int(row_lens[i])] for i in range(N)]
 
