@@ -267,6 +267,8 @@ def run_ours(args, cfg, file_lens):
 
     S, N, R = cfg["S"], cfg["N"], cfg["R"]
     mul_adds = N * R * (S // 2)
+    if args.comb_shape:
+        _lib.check(_lib.load().par2cuda_set_comb_shape(args.comb_shape), "set_comb_shape")
     job = ResidentJob(S, file_lens, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
     job.fill_synthetic(seed=1 + rank)
     torch.cuda.synchronize()
@@ -759,6 +761,8 @@ def main():
     ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor"], default="comb",
                     help="multiply-accumulate kernel of the resident-job workloads")
     ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")
+    ap.add_argument("--comb-shape", type=int, default=0,
+                    help="pin the comb kernel's CTA shape (par2cuda_set_comb_shape; 0 = automatic)")
     ap.add_argument("--inflight", type=int, default=8,
                     help="independent jobs in flight for the multi-job figure of hashing workloads (0/1 = skip)")
     ap.add_argument("--traffic-bytes", type=float, default=None,
