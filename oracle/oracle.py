@@ -28,9 +28,15 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
         os.makedirs(BUILD_DIR, exist_ok=True)
         tmp = LIB + ".tmp.%d" % os.getpid()
-        isa = ["-march=armv8-a+crc"] if os.uname().machine == "aarch64" else []
-        subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-pthread", "-std=gnu11", *isa,
-                               "-fno-strict-aliasing", "-o", tmp, SRC])
+        base = ["gcc", "-O3", "-fPIC", "-shared", "-pthread", "-std=gnu11", "-fno-strict-aliasing", "-o", tmp, SRC]
+        if os.uname().machine == "aarch64":
+            # CRC32 instructions; the SVE2 carry-less multiply baseline only if
+            # this compiler accepts it (the library checks the CPU at run time)
+            r = subprocess.run(base + ["-march=armv8-a+crc", "-DOR_ENABLE_SVE2"], capture_output=True)
+            if r.returncode != 0:
+                subprocess.check_call(base + ["-march=armv8-a+crc"])
+        else:
+            subprocess.check_call(base)
         os.replace(tmp, LIB)
     return LIB
 
@@ -58,6 +64,9 @@ def lib():
         L.or_recover_fast.restype = i32
         L.or_recover_fast.argtypes = [vp, ctypes.c_uint, sz, vp, ctypes.c_uint, vp, i32]
         L.or_fast_method.restype = ctypes.c_char_p
+        L.or_clmul_method.restype = ctypes.c_char_p
+        L.or_recover_clmul.restype = i32
+        L.or_recover_clmul.argtypes = [vp, ctypes.c_uint, sz, vp, ctypes.c_uint, vp, i32]
         L.or_crc32_fast.restype = ctypes.c_uint32; L.or_crc32_fast.argtypes = [vp, sz, ctypes.c_uint64]
         L.or_hash_rows.restype = None
         L.or_hash_rows.argtypes = [vp, sz, sz, vp, ctypes.c_uint, vp, vp, i32]
@@ -137,6 +146,21 @@ def recover_fast(inputs: np.ndarray, coeffs_rn: np.ndarray, threads: int = 1) ->
     rc = lib().or_recover_fast(_p(inputs), n, S, _p(c), c.shape[0], _p(out), threads)
     if rc:
         raise RuntimeError("oracle recover_fast failed: %d" % rc)
+    return out
+
+
+def recover_clmul(inputs: np.ndarray, coeffs_rn: np.ndarray, threads: int = 1):
+    """The carry-less multiply restatement (aarch64: SVE2 where the CPU has it,
+    else NEON); None where unavailable."""
+    inputs = np.ascontiguousarray(inputs, dtype=np.uint8)
+    n, S = inputs.shape
+    c = np.ascontiguousarray(coeffs_rn, dtype=np.uint16)
+    out = np.zeros((c.shape[0], S), dtype=np.uint8)
+    rc = lib().or_recover_clmul(_p(inputs), n, S, _p(c), c.shape[0], _p(out), threads)
+    if rc == -3:
+        return None
+    if rc:
+        raise RuntimeError("oracle recover_clmul failed: %d" % rc)
     return out
 
 

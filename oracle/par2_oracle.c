@@ -528,3 +528,285 @@ uint32_t or_crc32_fast(const uint8_t* data, size_t len, uint64_t zeroPad) {
 #else
 uint32_t or_crc32_fast(const uint8_t* data, size_t len, uint64_t zeroPad) { return or_crc32(data, len, zeroPad); }
 #endif
+
+/* ---------- CPU baseline: carry-less multiply method (SVE2) ----------
+ * Restates the reference's CLMUL_SVE2 method (gf16/gf16_clmul_sve2.c), its
+ * automatic choice on SVE2 hosts such as Grace: each 16-bit word a = a1 x^8 + a0
+ * times c = c1 x^8 + c0 as three 8x8 carry-less products (Karatsuba: a0c0,
+ * a1c1, (a0+a1)(c0+c1)) with PMULLB/PMULLT on the de-interleaved low/high
+ * bytes (even and odd words), accumulated unreduced over the inputs (the
+ * reduction is linear, so it is done once per output word at the end):
+ *     product = HH x^16 + (MM + LL + HH) x^8 + LL,   lo16 + hi16 x^16
+ *     result  = lo16 ^ red[hi16],   red[h] = h * x^16 mod 0x1100B (h < 2^15)
+ * Four inputs per pass into one output with the six accumulators (LL, MM, HH
+ * x even/odd) in registers, combined with three-input XORs.  Compiled only
+ * when the compiler accepts SVE2 (OR_ENABLE_SVE2, tried by the loader) and
+ * used only when the CPU reports SVE2. */
+#if defined(__aarch64__) && defined(OR_ENABLE_SVE2)
+#include <sys/auxv.h>
+#ifndef HWCAP2_SVE2
+#define HWCAP2_SVE2 (1 << 1)
+#endif
+#pragma GCC push_options
+#pragma GCC target("+sve2")
+#include <arm_sve.h>
+
+#define OR_CL_CHUNK 2048   /* words per unit: 4 inputs x 4 KiB + 12 KiB of accumulators in L1 */
+
+static uint16_t or_red_tab[32768];
+static pthread_once_t or_red_once = PTHREAD_ONCE_INIT;
+static void or_red_build(void) {
+	for(uint32_t h = 0; h < 32768; h++) or_red_tab[h] = or_mul((uint16_t)h, 0x100B);
+}
+
+typedef struct {
+	const uint8_t* inputs; const uint16_t* coeffs; unsigned n, r; size_t slice; uint8_t* out;
+	unsigned nthreads, tid;
+} or_cljob;
+
+static void* or_clmul_worker(void* arg) {
+	or_cljob* j = (or_cljob*)arg;
+	const size_t VLW = svcntb();                       /* words per svld2 block */
+	const size_t words = j->slice / 2;
+	const size_t vecWords = words / OR_CL_CHUNK * OR_CL_CHUNK;
+	const size_t nchunks = vecWords / OR_CL_CHUNK;
+	const size_t blocks = OR_CL_CHUNK / VLW;
+	uint8_t* accb = (uint8_t*)aligned_alloc(64, 6 * blocks * svcntb());
+	const svbool_t pt = svptrue_b8();
+	const size_t units = nchunks * j->r;
+	for(size_t u = j->tid; u < units; u += j->nthreads) {
+		const size_t ch = u / j->r;
+		const unsigned row = (unsigned)(u % j->r);
+		const size_t w0 = ch * OR_CL_CHUNK;
+		memset(accb, 0, 6 * blocks * svcntb());
+		for(unsigned i = 0; i < j->n; i += 4) {
+			const unsigned k = j->n - i < 4 ? j->n - i : 4;
+			const uint8_t* src[4];
+			uint16_t cv[4];
+			for(unsigned t = 0; t < 4; t++) {
+				cv[t] = t < k ? j->coeffs[(size_t)row * j->n + i + t] : 0;   /* zero: adds nothing */
+				src[t] = j->inputs + (size_t)(i + (t < k ? t : 0)) * j->slice + 2 * w0;
+			}
+			/* coefficient byte vectors (SVE types cannot form arrays) */
+			const svuint8_t a_c0 = svdup_n_u8((uint8_t)cv[0]), a_c1 = svdup_n_u8((uint8_t)(cv[0] >> 8)),
+			                a_cm = svdup_n_u8((uint8_t)(cv[0] ^ (cv[0] >> 8)));
+			const svuint8_t b_c0 = svdup_n_u8((uint8_t)cv[1]), b_c1 = svdup_n_u8((uint8_t)(cv[1] >> 8)),
+			                b_cm = svdup_n_u8((uint8_t)(cv[1] ^ (cv[1] >> 8)));
+			const svuint8_t c_c0 = svdup_n_u8((uint8_t)cv[2]), c_c1 = svdup_n_u8((uint8_t)(cv[2] >> 8)),
+			                c_cm = svdup_n_u8((uint8_t)(cv[2] ^ (cv[2] >> 8)));
+			const svuint8_t d_c0 = svdup_n_u8((uint8_t)cv[3]), d_c1 = svdup_n_u8((uint8_t)(cv[3] >> 8)),
+			                d_cm = svdup_n_u8((uint8_t)(cv[3] ^ (cv[3] >> 8)));
+			for(size_t b = 0; b < blocks; b++) {
+				uint8_t* ab = accb + 6 * b * svcntb();
+				svuint16_t lle = svld1_u16(pt, (const uint16_t*)(ab + 0 * svcntb()));
+				svuint16_t llo = svld1_u16(pt, (const uint16_t*)(ab + 1 * svcntb()));
+				svuint16_t mme = svld1_u16(pt, (const uint16_t*)(ab + 2 * svcntb()));
+				svuint16_t mmo = svld1_u16(pt, (const uint16_t*)(ab + 3 * svcntb()));
+				svuint16_t hhe = svld1_u16(pt, (const uint16_t*)(ab + 4 * svcntb()));
+				svuint16_t hho = svld1_u16(pt, (const uint16_t*)(ab + 5 * svcntb()));
+				/* inputs a, b, then c, d: two products per three-input XOR */
+#define OR_CL_PAIR(P, Q, SP, SQ) do { \
+					svuint8x2_t dp = svld2_u8(pt, (SP) + 2 * b * VLW); \
+					svuint8x2_t dq = svld2_u8(pt, (SQ) + 2 * b * VLW); \
+					svuint8_t p0 = svget2_u8(dp, 0), p1 = svget2_u8(dp, 1), pm = sveor_u8_x(pt, p0, p1); \
+					svuint8_t q0 = svget2_u8(dq, 0), q1 = svget2_u8(dq, 1), qm = sveor_u8_x(pt, q0, q1); \
+					lle = sveor3_u16(lle, svpmullb_u16(p0, P##_c0), svpmullb_u16(q0, Q##_c0)); \
+					llo = sveor3_u16(llo, svpmullt_u16(p0, P##_c0), svpmullt_u16(q0, Q##_c0)); \
+					hhe = sveor3_u16(hhe, svpmullb_u16(p1, P##_c1), svpmullb_u16(q1, Q##_c1)); \
+					hho = sveor3_u16(hho, svpmullt_u16(p1, P##_c1), svpmullt_u16(q1, Q##_c1)); \
+					mme = sveor3_u16(mme, svpmullb_u16(pm, P##_cm), svpmullb_u16(qm, Q##_cm)); \
+					mmo = sveor3_u16(mmo, svpmullt_u16(pm, P##_cm), svpmullt_u16(qm, Q##_cm)); \
+				} while(0)
+				OR_CL_PAIR(a, b, src[0], src[1]);
+				OR_CL_PAIR(c, d, src[2], src[3]);
+#undef OR_CL_PAIR
+				svst1_u16(pt, (uint16_t*)(ab + 0 * svcntb()), lle);
+				svst1_u16(pt, (uint16_t*)(ab + 1 * svcntb()), llo);
+				svst1_u16(pt, (uint16_t*)(ab + 2 * svcntb()), mme);
+				svst1_u16(pt, (uint16_t*)(ab + 3 * svcntb()), mmo);
+				svst1_u16(pt, (uint16_t*)(ab + 4 * svcntb()), hhe);
+				svst1_u16(pt, (uint16_t*)(ab + 5 * svcntb()), hho);
+			}
+		}
+		/* one reduction per output word */
+		uint8_t* dst = j->out + (size_t)row * j->slice + 2 * w0;
+		const size_t half = VLW / 2;                    /* 16-bit lanes per vector */
+		for(size_t b = 0; b < blocks; b++) {
+			const uint16_t* a = (const uint16_t*)(accb + 6 * b * svcntb());
+			for(size_t q = 0; q < half; q++)
+				for(unsigned odd = 0; odd < 2; odd++) {
+					const uint16_t ll = a[(0 + odd) * half + q], mm = a[(2 + odd) * half + q], hh = a[(4 + odd) * half + q];
+					const uint16_t mid = (uint16_t)(mm ^ ll ^ hh);
+					const uint16_t lo = (uint16_t)(ll ^ (uint16_t)(mid << 8));
+					const uint16_t hi = (uint16_t)(hh ^ (mid >> 8));
+					const uint16_t v = (uint16_t)(lo ^ or_red_tab[hi & 32767]);
+					const size_t w = b * VLW + 2 * q + odd;
+					dst[2 * w] = (uint8_t)v;
+					dst[2 * w + 1] = (uint8_t)(v >> 8);
+				}
+		}
+	}
+	free(accb);
+	return NULL;
+}
+#pragma GCC pop_options
+
+static int or_have_sve2(void) { return (getauxval(AT_HWCAP2) & HWCAP2_SVE2) != 0; }
+#endif
+
+#if defined(__aarch64__)
+/* The same method with NEON polynomial multiplies (the reference's
+ * CLMUL_NEON, gf16/gf16_clmul_neon.c, its automatic choice on NEON hosts
+ * without SVE2): vmull_p8 / vmull_high_p8 on the low and high eight words of
+ * the de-interleaved bytes, six products per input and 16 words, accumulated
+ * unreduced over four inputs per pass, one table reduction per output word. */
+#include <arm_neon.h>
+#ifndef OR_CL_CHUNK
+#define OR_CL_CHUNK 2048
+#endif
+static uint16_t or_nred_tab[32768];
+static pthread_once_t or_nred_once = PTHREAD_ONCE_INIT;
+static void or_nred_build(void) {
+	for(uint32_t h = 0; h < 32768; h++) or_nred_tab[h] = or_mul((uint16_t)h, 0x100B);
+}
+typedef struct {
+	const uint8_t* inputs; const uint16_t* coeffs; unsigned n, r; size_t slice; uint8_t* out;
+	unsigned nthreads, tid;
+} or_ncljob;
+
+static void* or_nclmul_worker(void* arg) {
+	or_ncljob* j = (or_ncljob*)arg;
+	const size_t words = j->slice / 2;
+	const size_t nchunks = words / OR_CL_CHUNK;
+	const size_t blocks = OR_CL_CHUNK / 16;
+	uint16_t* acc = (uint16_t*)aligned_alloc(64, blocks * 6 * 16 * sizeof(uint16_t)); /* per block: LL, MM, HH x 16 words */
+	const size_t units = nchunks * j->r;
+	for(size_t u = j->tid; u < units; u += j->nthreads) {
+		const size_t ch = u / j->r;
+		const unsigned row = (unsigned)(u % j->r);
+		const size_t w0 = ch * OR_CL_CHUNK;
+		memset(acc, 0, blocks * 6 * 16 * sizeof(uint16_t));
+		for(unsigned i = 0; i < j->n; i += 4) {
+			const unsigned k = j->n - i < 4 ? j->n - i : 4;
+			const uint8_t* src[4];
+			poly8x16_t c0[4], c1[4], cm[4];
+			for(unsigned t = 0; t < 4; t++) {
+				const uint16_t c = t < k ? j->coeffs[(size_t)row * j->n + i + t] : 0;   /* zero: adds nothing */
+				src[t] = j->inputs + (size_t)(i + (t < k ? t : 0)) * j->slice + 2 * w0;
+				c0[t] = vreinterpretq_p8_u8(vdupq_n_u8((uint8_t)c));
+				c1[t] = vreinterpretq_p8_u8(vdupq_n_u8((uint8_t)(c >> 8)));
+				cm[t] = vreinterpretq_p8_u8(vdupq_n_u8((uint8_t)(c ^ (c >> 8))));
+			}
+			for(size_t b = 0; b < blocks; b++) {
+				uint16_t* ab = acc + b * 96;
+				uint16x8_t ll0 = vld1q_u16(ab), ll1 = vld1q_u16(ab + 8);
+				uint16x8_t mm0 = vld1q_u16(ab + 16), mm1 = vld1q_u16(ab + 24);
+				uint16x8_t hh0 = vld1q_u16(ab + 32), hh1 = vld1q_u16(ab + 40);
+				for(unsigned t = 0; t < 4; t++) {
+					const uint8x16x2_t d = vld2q_u8(src[t] + 32 * b);
+					const poly8x16_t a0 = vreinterpretq_p8_u8(d.val[0]), a1 = vreinterpretq_p8_u8(d.val[1]);
+					const poly8x16_t am = vreinterpretq_p8_u8(veorq_u8(d.val[0], d.val[1]));
+					ll0 = veorq_u16(ll0, vreinterpretq_u16_p16(vmull_p8(vget_low_p8(a0), vget_low_p8(c0[t]))));
+					ll1 = veorq_u16(ll1, vreinterpretq_u16_p16(vmull_high_p8(a0, c0[t])));
+					hh0 = veorq_u16(hh0, vreinterpretq_u16_p16(vmull_p8(vget_low_p8(a1), vget_low_p8(c1[t]))));
+					hh1 = veorq_u16(hh1, vreinterpretq_u16_p16(vmull_high_p8(a1, c1[t])));
+					mm0 = veorq_u16(mm0, vreinterpretq_u16_p16(vmull_p8(vget_low_p8(am), vget_low_p8(cm[t]))));
+					mm1 = veorq_u16(mm1, vreinterpretq_u16_p16(vmull_high_p8(am, cm[t])));
+				}
+				vst1q_u16(ab, ll0); vst1q_u16(ab + 8, ll1);
+				vst1q_u16(ab + 16, mm0); vst1q_u16(ab + 24, mm1);
+				vst1q_u16(ab + 32, hh0); vst1q_u16(ab + 40, hh1);
+			}
+		}
+		uint8_t* dst = j->out + (size_t)row * j->slice + 2 * w0;
+		for(size_t b = 0; b < blocks; b++) {
+			const uint16_t* a = acc + b * 96;
+			for(unsigned q = 0; q < 16; q++) {
+				const uint16_t ll = a[q], mm = a[16 + q], hh = a[32 + q];
+				const uint16_t mid = (uint16_t)(mm ^ ll ^ hh);
+				const uint16_t lo = (uint16_t)(ll ^ (uint16_t)(mid << 8));
+				const uint16_t hi = (uint16_t)(hh ^ (mid >> 8));
+				const uint16_t v = (uint16_t)(lo ^ or_nred_tab[hi & 32767]);
+				const size_t w = b * 16 + q;
+				dst[2 * w] = (uint8_t)v;
+				dst[2 * w + 1] = (uint8_t)(v >> 8);
+			}
+		}
+	}
+	free(acc);
+	return NULL;
+}
+#endif
+
+/* Which carry-less multiply form or_recover_clmul uses on this host. */
+const char* or_clmul_method(void) {
+#if defined(__aarch64__) && defined(OR_ENABLE_SVE2)
+	if(or_have_sve2()) return "SVE2 carry-less multiply (restating the reference's CLMUL_SVE2 method, its automatic choice on SVE2 hosts)";
+#endif
+#if defined(__aarch64__)
+	return "NEON carry-less multiply (restating the reference's CLMUL_NEON method, its automatic choice on NEON hosts without SVE2)";
+#else
+	return "";
+#endif
+}
+
+/* The carry-less multiply method over zero-padded rows (SVE2 where the CPU
+ * has it, else NEON); returns -3 where it is not available (not aarch64). */
+int or_recover_clmul(const uint8_t* inputs, unsigned n, size_t slice, const uint16_t* coeffs, unsigned r,
+                     uint8_t* out, int threads) {
+#if defined(__aarch64__)
+	or_init();
+	if(slice & 1) return -1;
+	if(threads < 1) threads = 1;
+	if(threads > 256) threads = 256;
+#if defined(OR_ENABLE_SVE2)
+	const int sve2 = or_have_sve2();
+#else
+	const int sve2 = 0;
+#endif
+	if(!sve2) {
+		pthread_once(&or_nred_once, or_nred_build);
+		const size_t words = slice / 2, vecWords = words / OR_CL_CHUNK * OR_CL_CHUNK;
+		pthread_t th[256];
+		or_ncljob jobs[256];
+		for(int t = 0; t < threads; t++) {
+			or_ncljob jb = {inputs, coeffs, n, r, slice, out, (unsigned)threads, (unsigned)t};
+			jobs[t] = jb;
+		}
+		for(int t = 0; t < threads; t++) pthread_create(&th[t], NULL, or_nclmul_worker, &jobs[t]);
+		for(int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+		if(vecWords < words)
+			for(unsigned row = 0; row < r; row++) {
+				uint8_t* dst = out + (size_t)row * slice + 2 * vecWords;
+				memset(dst, 0, 2 * (words - vecWords));
+				for(unsigned i = 0; i < n; i++)
+					or_muladd_region(dst, inputs + (size_t)i * slice + 2 * vecWords, words - vecWords, coeffs[(size_t)row * n + i]);
+			}
+		return 0;
+	}
+#endif
+#if defined(__aarch64__) && defined(OR_ENABLE_SVE2)
+	pthread_once(&or_red_once, or_red_build);
+	const size_t words = slice / 2, vecWords = words / OR_CL_CHUNK * OR_CL_CHUNK;
+	pthread_t th[256];
+	or_cljob jobs[256];
+	for(int t = 0; t < threads; t++) {
+		or_cljob jb = {inputs, coeffs, n, r, slice, out, (unsigned)threads, (unsigned)t};
+		jobs[t] = jb;
+	}
+	for(int t = 0; t < threads; t++) pthread_create(&th[t], NULL, or_clmul_worker, &jobs[t]);
+	for(int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+	if(vecWords < words) { /* tail words with the table method */
+		for(unsigned row = 0; row < r; row++) {
+			uint8_t* dst = out + (size_t)row * slice + 2 * vecWords;
+			memset(dst, 0, 2 * (words - vecWords));
+			for(unsigned i = 0; i < n; i++)
+				or_muladd_region(dst, inputs + (size_t)i * slice + 2 * vecWords, words - vecWords, coeffs[(size_t)row * n + i]);
+		}
+	}
+	return 0;
+#else
+	(void)inputs; (void)n; (void)slice; (void)coeffs; (void)r; (void)out; (void)threads;
+	return -3;
+#endif
+}

@@ -37,3 +37,21 @@ def test_method_name():
     name = O.lib().or_fast_method().decode()
     if platform.machine() == "aarch64":
         assert "NEON" in name
+        assert "carry-less" in O.lib().or_clmul_method().decode()
+    print(O.lib().or_clmul_method().decode())
+
+
+@pytest.mark.parametrize("n,r,S,threads", [
+    (7, 3, 4096, 1), (33, 5, 2048 * 2 * 3 + 34, 4), (5, 2, 30, 2), (64, 9, 2048 * 2 * 5, 16), (1, 1, 4096, 3),
+])
+def test_clmul_recover_matches_oracle(n, r, S, threads):
+    """The carry-less multiply restatement (SVE2 or NEON form, whichever the
+    host runs) against the plain oracle: ragged input groups, word tails,
+    one input."""
+    rng = np.random.default_rng(n * 7 + r)
+    x = rng.integers(0, 256, size=(n, S), dtype=np.uint8)
+    c = rng.integers(0, 65536, size=(r, n), dtype=np.uint16)
+    got = O.recover_clmul(x, c, threads=threads)
+    if got is None:
+        pytest.skip("not an aarch64 host")
+    assert np.array_equal(got, O.recover_coeffs(x, np.full(n, S), c))
