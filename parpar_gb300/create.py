@@ -38,7 +38,6 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
-from . import _lib
 from . import par2packets as P
 from .job import ResidentJob
 
