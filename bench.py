@@ -35,6 +35,8 @@ UNIT = "mul-adds/s"
 
 # one ncu capture per contraction kernel on a 512-input x 512 KiB case:
 # dram__bytes_read.sum + dram__bytes_write.sum, and the algorithmic (N + R) x S
+# one ncu capture of k_file_md5 (4 files, 266.6 MB in all): DRAM bytes per byte hashed
+MD5_TRAFFIC = (272723456 + 4043776, 266590293)
 KERNEL_TRAFFIC = {
     "k_comb_pair": (270406912 + 87077120, (512 + 200) * 524288, "k_comb_pair<6,12,2> on 512x200x512KiB"),
     "k_comb_pair_rr": (268913408 + 81736448, (512 + 192) * 524288, "k_comb_pair_rr<8,12,2,152,56> on 512x192x512KiB"),
@@ -560,7 +562,10 @@ def run_ours(args, cfg, file_lens):
         line["roofline_md5"] = {
             "bound": "latency", "kernel": "k_file_md5", "achieved": big / (hash_ms / 1e3) / 1e6,
             "peak": md5_chain.value / 1e6, "unit": "MB/s per GPU thread (largest file's chain)",
-            "frac": big / (hash_ms / 1e3) / md5_chain.value, "traffic": None,
+            "frac": big / (hash_ms / 1e3) / md5_chain.value,
+            "traffic": MD5_TRAFFIC[0] / MD5_TRAFFIC[1] * sum(file_lens),
+            "traffic_source": "ncu dram__bytes_read+write of k_file_md5 on 4 files (%.1f MB for %.1f MB hashed), "
+                              "scaled by the bytes hashed" % (MD5_TRAFFIC[0] / 1e6, MD5_TRAFFIC[1] / 1e6),
             "peak_source": "measured: k_md5_chain, one MD5 stream on one thread with its data in registers"}
     # `roofline` is the kernel that bounds the step (the longest live kernel time)
     line["roofline"] = dict(line["roofline_md5"] if cfg["hashes"] and hash_ms > comb_ms else line["roofline_gf"])
