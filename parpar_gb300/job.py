@@ -241,15 +241,24 @@ class ResidentJob:
 
     # -------------------------------------------------------------- results
     def download(self, rec_host: torch.Tensor | None = None, stream=None):
-        """D2H of recovery slices, IFSC entries, file MD5s and checksum verdicts."""
+        """D2H of recovery slices, IFSC entries, file MD5s and checksum verdicts
+        (asynchronous on `stream`).  IFSC, MD5s and verdicts land in pinned
+        buffers owned by the job and reused by the next call."""
         st = stream or torch.cuda.current_stream(self.dev)
+        if not hasattr(self, "_h_small"):
+            # pinned host buffers made once: allocating pinned memory per call
+            # can synchronise the device and stall the next job's launches
+            self._h_small = (torch.empty_like(self.d_ifsc, device="cpu", pin_memory=True),
+                             torch.empty_like(self.d_fmd5, device="cpu", pin_memory=True),
+                             torch.empty_like(self.d_flags, device="cpu", pin_memory=True))
+        ifsc, fmd5, flags = self._h_small
         with torch.cuda.stream(st):
             if rec_host is None:
                 rec_host = torch.empty((self.R, self.S), dtype=torch.uint8, pin_memory=True)
             rec_host.copy_(self.d_rec.view(torch.uint8)[:, : self.S], non_blocking=True)
-            ifsc = self.d_ifsc.to("cpu", non_blocking=True)
-            fmd5 = self.d_fmd5.to("cpu", non_blocking=True)
-            flags = self.d_flags.to("cpu", non_blocking=True)
+            ifsc.copy_(self.d_ifsc, non_blocking=True)
+            fmd5.copy_(self.d_fmd5, non_blocking=True)
+            flags.copy_(self.d_flags, non_blocking=True)
         return rec_host, ifsc, fmd5, flags
 
     # -------------------------------------------------------------- PAR2 packets
