@@ -43,6 +43,19 @@ from .job import ResidentJob
 
 DEFAULT_CREATOR = "par2cuda (GB300 PAR2 recovery backend)"
 
+_PINNED: dict = {}
+
+
+def _pinned(key, rows: int, cols: int) -> torch.Tensor:
+    """A pinned host buffer of rows x cols bytes, kept for later calls:
+    pinning hundreds of MB per call costs more than the work it carries."""
+    n = rows * cols
+    t = _PINNED.get(key)
+    if t is None or t.numel() < n:
+        t = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+        _PINNED[key] = t
+    return t[:n].view(rows, cols)
+
 
 def js_round(x: float) -> int:
     """JavaScript Math.round for non-negative values (halves round up)."""
@@ -140,7 +153,7 @@ def _ingest(paths, sizes, job: ResidentJob, order, on_file=None, buf_rows: int =
     buffer; on_file(f) runs on the calling thread once the copy holding file
     f's last row has been issued."""
     S = job.S
-    bufs = [torch.empty((buf_rows, S), dtype=torch.uint8, pin_memory=True) for _ in range(nbuf)]
+    bufs = [_pinned(("ring", k), buf_rows, S) for k in range(nbuf)]
     free = [torch.cuda.Event() for _ in range(nbuf)]
     for e in free:
         e.record()
@@ -282,7 +295,7 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
 
     plan = plan_files(out_base, len(crit), recovery_slices, index=index)
     rec_md5 = job.recovery_packet_md5s(set_id) if recovery_slices else []
-    rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
+    rec_host = _pinned("rec", R, S)
     rec_host.copy_(job.d_rec.view(torch.uint8)[:, :S])
     rec_np = rec_host.numpy()
     def write(of):
