@@ -272,48 +272,81 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
         nums[first:first + n] = np.arange(off, off + n)
         off += n
     job.set_input_nums(nums)
-    job.run(hashes=True, file_md5=False)
+    job.run(hashes=True, file_md5=False)   # the current stream waits for the contraction, not the file MD5s
     mark("contraction+ifsc", job.sa)
-    job.file_md5_finish()
-    torch.cuda.synchronize()
-    mark("file_md5")
     if not bool(job.d_flags.all()):
         raise RuntimeError("recovery checksum verification failed")
 
+    # The recovery packets are written while the file MD5 chains still run:
+    # every packet's length is known now (the critical packets' contents wait
+    # for the file MD5s, their sizes do not), so each file is laid out at
+    # once and the recovery packets go to their offsets; the critical packets
+    # fill their places when the MD5s are in.
     ifsc = job.d_ifsc.cpu().numpy().reshape(job.N, 20)
-    fmd5 = job.d_fmd5.cpu().numpy().reshape(len(paths), 16)
     main, set_id = P.main_packet(S, ids)
-    crit = []
-    for f in order:
-        crit.append(P.filedesc_packets(set_id, ids[f], fmd5[f].tobytes(), m16[f], sizes[f], names[f]))
-        if sizes[f]:
-            first = int(job.first_row[f])
-            n = (sizes[f] + S - 1) // S
-            crit.append(P.ifsc_packet(set_id, ids[f], ifsc[first:first + n].tobytes()))
-    crit.append(main)
-    creator_pkt = P.creator_packet(set_id, creator)
+    zero16 = bytes(16)
 
-    plan = plan_files(out_base, len(crit), recovery_slices, index=index)
+    def critical(fmd5_of):
+        out = []
+        for f in order:
+            out.append(P.filedesc_packets(set_id, ids[f], fmd5_of(f), m16[f], sizes[f], names[f]))
+            if sizes[f]:
+                first = int(job.first_row[f])
+                n = (sizes[f] + S - 1) // S
+                out.append(P.ifsc_packet(set_id, ids[f], ifsc[first:first + n].tobytes()))
+        out.append(main)
+        return out
+
+    crit_len = [len(c) for c in critical(lambda f: zero16)]
+    creator_pkt = P.creator_packet(set_id, creator)
+    plan = plan_files(out_base, len(crit_len), recovery_slices, index=index)
+    rec_len = 68 + S
+    layouts = []                      # per file: [(offset, kind, k)]
+    for of in plan:
+        pos, lay = 0, []
+        for kind, k in of.packets:
+            lay.append((pos, kind, k))
+            pos += crit_len[k] if kind == "crit" else (len(creator_pkt) if kind == "creator" else rec_len)
+        layouts.append((of.name, pos, lay))
     rec_md5 = job.recovery_packet_md5s(set_id) if recovery_slices else []
     rec_host = _pinned("rec", R, S)
     rec_host.copy_(job.d_rec.view(torch.uint8)[:, :S])
     rec_np = rec_host.numpy()
-    def write(of):
-        # recovery packets: 68-byte header, then the slice straight from the
-        # pinned buffer (no per-packet copies)
-        with open(of.name, "wb") as fh:
-            for kind, k in of.packets:
-                if kind == "crit":
-                    fh.write(crit[k])
-                elif kind == "creator":
-                    fh.write(creator_pkt)
-                else:
-                    fh.write(P.recovery_header(set_id, k, S, rec_md5[k]))
-                    fh.write(memoryview(rec_np[k]))
-        return of.name
+
+    def write_recovery(item):
+        name, total, lay = item
+        fd = os.open(name, os.O_WRONLY | os.O_CREAT | os.O_TRUNC, 0o644)
+        try:
+            os.ftruncate(fd, total)
+            for pos, kind, k in lay:
+                if kind == "recovery":
+                    os.pwrite(fd, P.recovery_header(set_id, k, S, rec_md5[k]), pos)
+                    os.pwrite(fd, memoryview(rec_np[k]), pos + 68)
+        finally:
+            os.close(fd)
+        return name
 
     from concurrent.futures import ThreadPoolExecutor
-    with ThreadPoolExecutor(max_workers=min(8, len(plan))) as ex:
-        written = list(ex.map(write, plan))
+    with ThreadPoolExecutor(max_workers=min(8, len(layouts))) as ex:
+        written = list(ex.map(write_recovery, layouts))
+    mark("recovery written")
+
+    job.file_md5_finish()
+    torch.cuda.synchronize()
+    mark("file_md5")
+    fmd5 = job.d_fmd5.cpu().numpy().reshape(len(paths), 16)
+    crit = critical(lambda f: fmd5[f].tobytes())
+    if [len(c) for c in crit] != crit_len:
+        raise RuntimeError("critical packet sizes changed")
+    for name, total, lay in layouts:
+        fd = os.open(name, os.O_WRONLY)
+        try:
+            for pos, kind, k in lay:
+                if kind == "crit":
+                    os.pwrite(fd, crit[k], pos)
+                elif kind == "creator":
+                    os.pwrite(fd, creator_pkt, pos)
+        finally:
+            os.close(fd)
     mark("written")
     return written
