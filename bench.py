@@ -461,7 +461,7 @@ def run_ours(args, cfg, file_lens):
                 with torch.cuda.stream(ctx[k]):
                     if upload is not None:
                         jk.upload(upload)
-                    jk.run(hashes=True)
+                    jk.run(hashes=True, packed_md5=True)
                     if down is not None:
                         jk.download(down[k])
             for c in ctx:
@@ -480,7 +480,8 @@ def run_ours(args, cfg, file_lens):
         inflight = {"jobs_in_flight": len(jobs_k), "value": mul_adds * len(jobs_k) * world / (ims / 1e3), "unit": UNIT,
                     "ms_per_round": ims, "jobs_per_s": len(jobs_k) * world / (ims / 1e3),
                     "desc": "%d independent jobs of this workload (distinct seeded inputs, each resident) per round, "
-                            "each on its own stream; whole pass per job incl. IFSC + file MD5" % len(jobs_k)}
+                            "each on its own stream; whole pass per job incl. IFSC + file MD5 (chains packed 32 per "
+                            "warp so that they leave the other SMs to the other jobs)" % len(jobs_k)}
         if e2e is not None:
             downs = [torch.empty((R, S), dtype=torch.uint8, pin_memory=True) for _ in jobs_k]
             round_(host_in, downs)

@@ -197,6 +197,11 @@ int par2cuda_file_md5(const void* d_rows, size_t pitch_bytes, unsigned num_files
                       const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, void* stream) {
 	return p2c::file_md5(d_rows, pitch_bytes, num_files, d_file_len, d_first_row, slice_bytes, d_md5, (cudaStream_t)stream);
 }
+int par2cuda_file_md5_packed(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
+                             const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, void* stream) {
+	return p2c::file_md5(d_rows, pitch_bytes, num_files, d_file_len, d_first_row, slice_bytes, d_md5, (cudaStream_t)stream,
+	                     true);
+}
 int par2cuda_rows_md5(const void* d_rows, size_t pitch_bytes, unsigned num_rows, size_t data_len,
                       const uint8_t* d_prefix, unsigned prefix_len, uint8_t* d_md5, void* stream) {
 	return p2c::rows_md5(d_rows, pitch_bytes, num_rows, data_len, d_prefix, prefix_len, d_md5, (cudaStream_t)stream);

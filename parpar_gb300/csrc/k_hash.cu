@@ -328,12 +328,17 @@ __global__ void __launch_bounds__(32) k_file_md5(const uint8_t* rows, size_t pit
 }
 
 int file_md5(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen, const uint32_t* dFirstRow,
-             size_t sliceBytes, uint8_t* dOut, cudaStream_t st)
+             size_t sliceBytes, uint8_t* dOut, cudaStream_t st, bool packed)
 {
 	if(!nFiles) return 0;
 	if(pitchBytes % 16) { set_error("row pitch must be a multiple of 16 bytes"); return -1; }
-	// one thread per file, one file per warp-slot: spread files over SMs
-	k_file_md5<<<nFiles, 1, 0, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen, dFirstRow, sliceBytes, dOut);
+	// one thread per file.  Default: one file per block, spread over SMs (the
+	// fastest chains: 108 MB/s).  Packed: 32 files per warp, ~6 % slower per
+	// chain but ceil(nFiles/32) blocks instead of nFiles, each of which keeps a
+	// full-register-file CTA of other work off its SM while the chains run.
+	const unsigned lanes = packed ? 32u : 1u;
+	k_file_md5<<<(nFiles + lanes - 1) / lanes, lanes, 0, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen,
+	                                                          dFirstRow, sliceBytes, dOut);
 	P2C_CUDA_TRY(cudaGetLastError());
 	return 0;
 }

@@ -211,9 +211,11 @@ class ResidentJob:
         if hashes:
             self.file_md5_finish()
 
-    def run(self, hashes: bool = True, file_md5: bool = True):
+    def run(self, hashes: bool = True, file_md5: bool = True, packed_md5: bool = False):
         """Issues the whole job on streams A and B (asynchronous); file_md5 =
-        False when the file MD5s were already launched (file_md5_async)."""
+        False when the file MD5s were already launched (file_md5_launch);
+        packed_md5 packs the file MD5 chains 32 per warp (several jobs in
+        flight: the chains then leave the other SMs to the other jobs)."""
         L = self.L
         cur = torch.cuda.current_stream(self.dev)
         self.sa.wait_stream(cur)
@@ -226,8 +228,9 @@ class ResidentJob:
         if hashes and file_md5:
             # the file MD5s (long serial chains) start at once on B: they read
             # only each file's own bytes, not the padding A writes
-            _lib.check(L.par2cuda_file_md5(self.d_in.data_ptr(), self.pitch, len(self.file_lens), self.d_flen.data_ptr(),
-                                          self.d_first.data_ptr(), self.S, self.d_fmd5.data_ptr(), b), "file_md5")
+            md5 = L.par2cuda_file_md5_packed if packed_md5 else L.par2cuda_file_md5
+            _lib.check(md5(self.d_in.data_ptr(), self.pitch, len(self.file_lens), self.d_flen.data_ptr(),
+                           self.d_first.data_ptr(), self.S, self.d_fmd5.data_ptr(), b), "file_md5")
         _lib.check(L.par2cuda_muladd(self.d_in.data_ptr(), self.pw, self.N, self.d_coeff.data_ptr(), self.d_rec.data_ptr(),
                                     self.pw, self.R, self.row_words, 0, self.method, self.d_scratch.data_ptr(),
                                     self.scratch_bytes, a), "muladd")

@@ -114,3 +114,29 @@ def test_rows_md5_with_packet_prefix():
     got = out.cpu().numpy().reshape(n, 16)
     for i in range(n):
         assert got[i].tobytes() == hashlib.md5(pre[i].tobytes() + bufs[i].tobytes()).digest()
+
+
+def test_packed_file_md5_matches_unpacked():
+    """par2cuda_file_md5_packed (32 chains per warp) gives the same digests as
+    the one-chain-per-block launch, for 40 uneven files including a 1-byte one."""
+    torch = pytest.importorskip("torch")
+    from parpar_gb300 import _lib
+    from parpar_gb300.job import ResidentJob
+    S = 4096
+    rng = np.random.default_rng(40)
+    lens = [int(x) for x in rng.integers(1, 40 * S, size=39)] + [1]
+    job = ResidentJob(S, lens, [0])
+    job.fill_synthetic(5)
+    L = _lib.load()
+    outs = []
+    for fn in (L.par2cuda_file_md5, L.par2cuda_file_md5_packed):
+        d = torch.zeros(16 * len(lens), dtype=torch.uint8, device="cuda")
+        _lib.check(fn(job.d_in.data_ptr(), job.pitch, len(lens), job.d_flen.data_ptr(), job.d_first.data_ptr(), S,
+                      d.data_ptr(), None), "md5")
+        outs.append(d.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    rows = job.d_in.view(torch.uint8).cpu().numpy()
+    f = 7
+    a = int(job.first_row[f])
+    data = rows[a:a + (lens[f] + S - 1) // S, :S].reshape(-1)[:lens[f]]
+    assert outs[0][16 * f:16 * f + 16].tobytes() == O.md5(data)
