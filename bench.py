@@ -158,102 +158,193 @@ def whole_job_value(units_per_rank: float, ms: float, world: int) -> float:
 
 
 # ---------------------------------------------------------------------------- CPU
-def cpu_baseline_run(cfg, file_lens, threads, window=32768, seed=1):
-    """The reference algorithm's CPU implementation on a bounded sample of the
-    step: every input x every recovery slice over a `window`-byte window of
-    each slice, plus the MD5/CRC32 work over the same bytes, scaled to the full
-    step.  The multiply uses the oracle's fastest restatement on this host (the
-    reference's NEON split-nibble shuffle on aarch64, its LOOKUP method
-    elsewhere), checked against the plain oracle before timing."""
+class CpuJob:
+    """One job of the workload in host memory for the CPU legs: the same seeded
+    bytes as the GPU arm's rows (parpar_gb300.synth, generated by the oracle's
+    C filler), the slice layout of the files, and the output buffers.  Nothing
+    here loads a library of this repository's product."""
+
+    def __init__(self, cfg, file_lens, seed=1):
+        from oracle import oracle as O
+        from parpar_gb300.layout import file_layout
+        self.S, self.N, self.R = cfg["S"], cfg["N"], cfg["R"]
+        self.hashes = cfg["hashes"]
+        self.file_lens = np.array(file_lens, dtype=np.uint64)
+        self.first_row, row_lens = file_layout(file_lens, self.S)
+        self.lens = row_lens.astype(np.uint64)
+        self.x = O.synth_rows(seed, 0, self.N, self.S)
+        self.nums = np.arange(self.N, dtype=np.uint16)
+        self.exps = np.arange(self.R, dtype=np.uint16)
+        self.out = np.zeros((self.R, self.S), dtype=np.uint8)
+        self.valid = np.zeros(self.R, dtype=np.int32)
+        self.ifsc = np.zeros(self.N * 20, dtype=np.uint8)
+        self.fmd5 = np.zeros(max(1, len(file_lens)) * 16, dtype=np.uint8)
+        self.mul_adds = self.N * self.R * (self.S // 2)
+
+
+def reference_core():
+    """The reference's own CPU core compiled on this host (oracle/_ref), or
+    None and the reason it is not there."""
+    import ctypes
+    from oracle import refsrc
+    if not os.path.exists(refsrc.REF_LIB):
+        err = os.path.join(refsrc.REF_OUT, "build_error.txt")
+        why = open(err).read().strip().splitlines()[0] if os.path.exists(err) else \
+            "reference sources not staged on this host (oracle/_ref/src)"
+        return None, why
+    L = ctypes.CDLL(refsrc.REF_LIB)
+    vp, sz, u = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint
+    L.ref_job.restype = ctypes.c_int
+    L.ref_job.argtypes = [vp, sz, vp, vp, u, sz, vp, u, vp, vp, vp, vp, u, vp, vp, ctypes.c_int,
+                          ctypes.POINTER(ctypes.c_double)]
+    L.ref_host_info.restype = ctypes.c_int
+    L.ref_host_info.argtypes = [ctypes.c_char_p, sz]
+    L.ref_last_method_name.restype = ctypes.c_char_p
+    return L, None
+
+
+def _reference_step(L, job, threads):
+    """One whole job through ParPar's PAR2Proc + PAR2ProcCPU (GF16_AUTO) with
+    its HasherInput per file concurrently (oracle/ref_shim.cpp ref_job);
+    returns (wall, gf, hash) seconds."""
+    import ctypes
+    from oracle.oracle import _p
+    t = (ctypes.c_double * 3)()
+    nf = len(job.file_lens) if job.hashes else 0
+    rc = L.ref_job(_p(job.x), job.S, _p(job.lens), _p(job.nums), job.N, job.S, _p(job.exps), job.R, _p(job.out),
+                   _p(job.valid), _p(job.file_lens), _p(job.first_row), nf, _p(job.ifsc), _p(job.fmd5), threads, t)
+    if rc != 0:
+        raise RuntimeError("reference job failed: %d" % rc)
+    if not job.valid.all():
+        raise RuntimeError("reference checksum verdict false")
+    return t[0], t[1], t[2]
+
+
+def _port_step(job, threads):
+    """The oracle's restatement of the reference's automatic SIMD method on
+    this host (used only where the reference core did not build): the GF
+    multiply-accumulate over `threads` threads and, concurrently, each file's
+    IFSC + file MD5 on a thread of its own, as the reference runs them."""
+    import concurrent.futures as cf
     from oracle import oracle as O
-    from parpar_gb300 import synth
-    from parpar_gb300.job import file_layout, par2_coefficients
-    S, N, R = cfg["S"], cfg["N"], cfg["R"]
-    W = min(window, S)
-    _, row_lens = file_layout(file_lens, S)
-    x = synth.slices(seed, 0, N, W)
-    lens = np.minimum(row_lens, W).astype(np.uint64)
-    for i in range(N):
-        x[i, lens[i]:] = 0
-    coeffs = par2_coefficients(np.arange(N), list(range(R)))
-    n0, r0, w0 = min(N, 24), min(R, 5), min(W, 3 * 4096 + 34)
-    chk = np.ascontiguousarray(x[:n0, :w0])
-    want = O.recover_coeffs(chk, np.full(n0, w0), coeffs[:r0, :n0])
-    # every restatement of the reference's SIMD methods available on this host,
-    # checked against the plain oracle, timed; the fastest is the baseline
-    cands = [(O.lib().or_clmul_method().decode(), O.recover_clmul),
-             (O.lib().or_fast_method().decode(), O.recover_fast)]
-    timed = []
-    for name, fn in cands:
-        got = fn(chk, coeffs[:r0, :n0], threads=2)
-        if got is None:
-            continue
-        if not np.array_equal(got, want):
-            raise RuntimeError("CPU baseline multiply (%s) disagrees with the oracle" % name)
-        t0 = time.perf_counter()
-        fn(x, coeffs, threads=threads)
-        timed.append((time.perf_counter() - t0, name))
-    t_gf, gf_method = min(timed)
-    others = "; ".join("%s: %.3f s" % (nm, t) for t, nm in timed if nm != gf_method)
-    t_hash = 0.0
-    chain_s = 0.0
-    if cfg["hashes"]:
-        lib = O.lib()
-        md5 = np.zeros((N, 16), np.uint8)
-        crc = np.zeros(N, np.uint32)
-        t0 = time.perf_counter()
-        lib.or_hash_rows(O._p(x), W, W, None, N, O._p(md5), O._p(crc), threads)  # slice lane: MD5 + CRC
-        lib.or_hash_rows(O._p(x), W, W, None, N, O._p(md5), None, threads)      # file lane: MD5
-        t_hash = time.perf_counter() - t0
-        # the reference hashes each file on one thread (slice MD5 and file MD5
-        # as one two-lane pass, CRC32 in hardware): the largest file is a
-        # serial floor, taken at the one-thread rate of a single MD5 lane
-        k = max(1, min(N, (16 << 20) // W))
-        t0 = time.perf_counter()
-        lib.or_hash_rows(O._p(x), W, W, None, k, O._p(md5), None, 1)
-        chain_s = max(file_lens) / (k * W / (time.perf_counter() - t0))
-    scale = S / W
-    step = max((t_gf + t_hash) * scale, chain_s)
-    mul_adds = N * R * (S // 2)
-    return {"value": mul_adds / step, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d inputs x %d recovery over a %d-byte window of each %d-byte slice%s, scaled x%.0f to the step%s"
-                      % (N, R, W, S, " + MD5/CRC32 of the same bytes" if cfg["hashes"] else "", scale,
-                         "; step = max(that, largest file %.0f MB / one-thread MD5 rate = %.3f s)"
-                         % (max(file_lens) / 1e6, chain_s) if cfg["hashes"] else ""),
-            "method": "%s, %d threads%s" % (gf_method, threads, " (also timed: %s)" % others if others else ""),
-            "step_s_est": step, "sample_s": t_gf + t_hash}
+    if not hasattr(job, "coeffs"):
+        job.coeffs = O.par2_coeff_matrix(job.nums, job.exps)
+        for i in range(job.N):   # the restatement takes zero-padded rows
+            job.x[i, int(job.lens[i]):] = 0
+        job.port_fn, job.port_name = ((O.recover_clmul, O.lib().or_clmul_method().decode())
+                                      if O.recover_clmul(job.x[:2, :64], job.coeffs[:1, :2]) is not None
+                                      else (O.recover_fast, O.lib().or_fast_method().decode()))
+    t0 = time.perf_counter()
+    hash_t = [0.0]
+
+    def hash_all():
+        def one(f):
+            a = int(job.first_row[f])
+            n = max(1, (int(job.file_lens[f]) + job.S - 1) // job.S)
+            O.hash_file(job.x[a:a + n].reshape(-1)[: int(job.file_lens[f])], job.S)
+        with cf.ThreadPoolExecutor(max_workers=len(job.file_lens)) as ex:
+            list(ex.map(one, range(len(job.file_lens))))
+        hash_t[0] = time.perf_counter() - t0
+    th = threading.Thread(target=hash_all) if job.hashes else None
+    if th:
+        th.start()
+    job.out[:] = job.port_fn(job.x, job.coeffs, threads=threads)
+    t_gf = time.perf_counter() - t0
+    if th:
+        th.join()
+    return time.perf_counter() - t0, t_gf, hash_t[0]
+
+
+def cpu_step_fn(threads):
+    """(step function(job) -> (wall, gf, hash) seconds, description dict) of the
+    best available CPU path: the reference's own core where it built on this
+    host, else the oracle's port of its automatic method."""
+    L, why = reference_core()
+    if L is not None:
+        import ctypes
+        buf = ctypes.create_string_buffer(512)
+        L.ref_host_info(buf, 512)
+        info = dict(kv.split("=", 1) for kv in buf.value.decode().split(";") if "=" in kv)
+        host = buf.value.decode().split(";")[-1]
+        desc = {"kind": "reference", "cores": threads,
+                "method": "ParPar PAR2ProcCPU, GF16_AUTO -> %s, %d threads; HasherInput per file (%s)"
+                          % (info.get("method", "?"), threads, host)}
+        return (lambda job: _reference_step(L, job, threads)), desc
+    desc = {"kind": "port", "cores": threads, "reference_unavailable": why}
+
+    def step(job):
+        r = _port_step(job, threads)
+        desc["method"] = "%s, %d threads (oracle restatement of the reference's automatic method)" % (job.port_name, threads)
+        return r
+    return step, desc
+
+
+def cpu_baseline_run(cfg, file_lens, threads, steps=1):
+    """cpu_baseline of the GPU arm's line: whole jobs of the workload through
+    the best available CPU path (cpu_step_fn), `steps` of them after one
+    untimed warm-up job."""
+    job = CpuJob(cfg, file_lens)
+    step, desc = cpu_step_fn(threads)
+    step(job)
+    walls = [step(job)[0] for _ in range(steps)]
+    t = float(np.mean(walls))
+    out = dict(desc)
+    out.update({"value": job.mul_adds / t, "unit": UNIT,
+                "sample": "%d whole job(s) of the workload (%d inputs x %d recovery x %d bytes%s), %.2f s each"
+                          % (steps, job.N, job.R, job.S, " + IFSC + file MD5 per file" if job.hashes else "", t)})
+    return out
 
 
 def run_reference(args, cfg, file_lens):
+    """--impl reference: the reference's CPU implementation of the path on this
+    host's cores, one whole job per step, on the GPU arm's config, metric and
+    unit.  Under torchrun only rank 0 measures."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    vals, samples = [], None
+    job = CpuJob(cfg, file_lens)
+    step, desc = cpu_step_fn(threads)
     for _ in range(args.warmup):
-        cpu_baseline_run(cfg, file_lens, threads, window=args.cpu_window)
+        step(job)
+    walls, gfs, hashes = [], [], []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r = cpu_baseline_run(cfg, file_lens, threads, window=args.cpu_window)
-        vals.append(r["value"])
-        samples = r
+        w, g, h = step(job)
+        walls.append(w)
+        gfs.append(g)
+        hashes.append(h)
     wall = time.perf_counter() - t0
-    value = float(np.median(vals))
-    mul_adds = cfg["N"] * cfg["R"] * (cfg["S"] // 2)
+    ms = wall / args.steps * 1e3
+    value = job.mul_adds / (ms / 1e3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mul_adds / value * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16 GF(2^16)",
         "data": "synthetic (seeded splitmix64 slices)",
-        "config": {"workload": args.workload, "desc": cfg["desc"], "slice_bytes": cfg["S"], "inputs": cfg["N"],
-                   "recovery": cfg["R"], "files": len(file_lens)},
-        "cpu_baseline": {k: samples[k] for k in ("value", "unit", "cores", "kind", "sample", "method")},
+        "config": bench_config(args, cfg, file_lens, world),
+        "src_GBps_x_recovery": job.N * job.S * job.R / (ms / 1e3) / 1e9,
+        "p50_latency_s": float(np.percentile(walls, 50)), "p99_latency_s": float(np.percentile(walls, 99)),
+        "cpu_parts_s": {"gf_mean": float(np.mean(gfs)), "hash_mean": float(np.mean(hashes))},
+        "cpu_baseline": dict(desc, value=value, unit=UNIT,
+                             sample="every step is one whole job of the workload (%d inputs x %d recovery x %d bytes%s); "
+                                    "jobs run back to back" % (job.N, job.R, job.S,
+                                                               " + IFSC + file MD5 per file" if job.hashes else "")),
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": wall,
     }
-    line["cpu_baseline"]["value"] = value
     print(json.dumps(line))
     return 0
+
+
+def bench_config(args, cfg, file_lens, world):
+    """The `config` object of both arms' lines (identical for the same run)."""
+    S, N = cfg["S"], cfg["N"]
+    return {"workload": args.workload, "desc": cfg["desc"], "slice_bytes": S, "inputs": N, "recovery": cfg["R"],
+            "files": len(file_lens),
+            "l2": "inputs (%.1f GiB per job) larger than L2 (129 MB); no flush" % (N * S / 2**30),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 # ---------------------------------------------------------------------------- GPU
@@ -526,9 +617,7 @@ def run_ours(args, cfg, file_lens):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u16 GF(2^16)", "data": "synthetic (seeded splitmix64 slices), inputs resident in HBM",
-        "config": {"workload": args.workload, "desc": cfg["desc"], "slice_bytes": S, "inputs": N, "recovery": R,
-                   "files": len(file_lens), "l2": "inputs (%.1f GiB) larger than L2 (129 MB); no flush" % (N * S / 2**30),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": bench_config(args, cfg, file_lens, world),
         "src_GBps_x_recovery": N * S * R * world / (ms / 1e3) / 1e9,
         "kernels_ms": {"muladd": comb_ms, "file_md5": hash_ms, "step": ms},
         "method": args.method,
@@ -571,8 +660,7 @@ def run_ours(args, cfg, file_lens):
     # `roofline` is the kernel that bounds the step (the longest live kernel time)
     line["roofline"] = dict(line["roofline_md5"] if cfg["hashes"] and hash_ms > comb_ms else line["roofline_gf"])
     if not args.no_cpu_baseline and world == 1:
-        cb = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1, window=args.cpu_window)
-        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "method")}
+        line["cpu_baseline"] = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1)
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
@@ -696,8 +784,7 @@ def run_create_workload(args, cfg):
         "gpu_launches": None,
     }
     if not args.no_cpu_baseline:
-        cb = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1, window=args.cpu_window)
-        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "method")}
+        line["cpu_baseline"] = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1)
     print(json.dumps(line))
     return 0
 
@@ -774,7 +861,6 @@ def main():
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-plugin", action="store_true", help="skip the plugin-boundary e2e measurement")
     ap.add_argument("--plugin-steps", type=int, default=2)
-    ap.add_argument("--cpu-window", type=int, default=262144)
     ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor"], default="comb",
                     help="multiply-accumulate kernel of the resident-job workloads")
     ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")

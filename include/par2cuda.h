@@ -4,10 +4,11 @@
  * One handle = one backend instance on one CUDA device, the counterpart of a
  * PAR2ProcOCL / PAR2ProcCPU object behind ParPar's backend plugin interface
  * IPAR2ProcBackend (gf16/controller.h:77-217).  Each entry point below names
- * the reference member it replaces.  A C++ adapter class deriving from
- * IPAR2ProcBackend forwards its virtuals to these functions,
- * so PAR2Proc (gf16/controller.cpp) and the node addon (src/gf.cc) drive it
- * unchanged.
+ * the reference member it replaces.  The C++ adapter class PAR2ProcCUDA
+ * (parpar_gb300/adapter/controller_cuda.{h,cpp}, which becomes
+ * gf16/controller_cuda.{h,cpp} in a ParPar tree) derives from IPAR2ProcBackend
+ * and forwards its virtuals to these functions, so PAR2Proc
+ * (gf16/controller.cpp) and the node addon (src/gf.cc) drive it unchanged.
  *
  * Conventions
  *  - Plain pointers and sizes only.  Host buffers may be pageable or pinned;

@@ -70,6 +70,8 @@ def lib():
         L.or_crc32_fast.restype = ctypes.c_uint32; L.or_crc32_fast.argtypes = [vp, sz, ctypes.c_uint64]
         L.or_hash_rows.restype = None
         L.or_hash_rows.argtypes = [vp, sz, sz, vp, ctypes.c_uint, vp, vp, i32]
+        L.or_synth_fill.restype = None
+        L.or_synth_fill.argtypes = [vp, sz, ctypes.c_uint, sz, ctypes.c_uint64, ctypes.c_uint64, i32]
         _lib = L
     return _lib
 
@@ -162,6 +164,23 @@ def recover_clmul(inputs: np.ndarray, coeffs_rn: np.ndarray, threads: int = 1):
     if rc:
         raise RuntimeError("oracle recover_clmul failed: %d" % rc)
     return out
+
+
+def synth_rows(seed: int, first: int, count: int, nbytes: int, threads: int = 0) -> np.ndarray:
+    """uint8[count, nbytes]: the bytes of parpar_gb300.synth.slices(seed, first, count, nbytes),
+    generated in C over `threads` threads (all host cores by default)."""
+    out = np.empty((count, nbytes), dtype=np.uint8)
+    lib().or_synth_fill(_p(out), nbytes, count, nbytes, seed, first, threads or (os.cpu_count() or 1))
+    return out
+
+
+def par2_coeff_matrix(input_nums, exps) -> np.ndarray:
+    """[R][N] uint16 PAR2 coefficients 2^(log_i * e) from the oracle's tables."""
+    L = lib()
+    logs = np.array([L.or_input_log(int(i)) for i in input_nums], dtype=np.int64)
+    expt = np.array([L.or_exp(k) for k in range(65535)], dtype=np.uint16)
+    e = np.asarray(exps, dtype=np.int64)
+    return expt[(e[:, None] * logs[None, :]) % 65535]
 
 
 def coeff(i: int, e: int) -> int:

@@ -353,6 +353,39 @@ void or_hash_file(const uint8_t* data, size_t len, size_t sliceSize, uint8_t* if
 
 uint32_t or_crc32_fast(const uint8_t* data, size_t len, uint64_t zeroPad);
 
+/* ---------- seeded synthetic slices (the bytes of parpar_gb300/synth.py) ----------
+ * Byte b of row `first + i` is byte b % 8 of splitmix64(seed*K1 + row*K2 + b/8);
+ * filled over `threads` threads so the CPU arm can build multi-GiB inputs. */
+typedef struct { uint8_t* dst; size_t pitch, bytes; unsigned n, nt, tid; uint64_t seed, first; } or_sjob;
+static void* or_sworker(void* arg) {
+	const or_sjob* j = (const or_sjob*)arg;
+	for(unsigned i = j->tid; i < j->n; i += j->nt) {
+		uint64_t base = j->seed * 0xD1342543DE82EF95ull + (j->first + i) * 0x9E3779B97F4A7C15ull;
+		uint8_t* row = j->dst + (size_t)i * j->pitch;
+		for(size_t u = 0; u * 8 < j->bytes; u++) {
+			uint64_t z = base + u;
+			z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+			z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+			z ^= z >> 31;
+			size_t k = j->bytes - u * 8 < 8 ? j->bytes - u * 8 : 8;
+			for(size_t b = 0; b < k; b++) row[u * 8 + b] = (uint8_t)(z >> (8 * b));
+		}
+	}
+	return NULL;
+}
+void or_synth_fill(uint8_t* dst, size_t pitch, unsigned n, size_t bytes, uint64_t seed, uint64_t first, int threads) {
+	if(threads < 1) threads = 1;
+	if(threads > 256) threads = 256;
+	pthread_t th[256];
+	or_sjob jobs[256];
+	for(int t = 0; t < threads; t++) {
+		or_sjob jb = {dst, pitch, bytes, n, (unsigned)threads, (unsigned)t, seed, first};
+		jobs[t] = jb;
+	}
+	for(int t = 0; t < threads; t++) pthread_create(&th[t], NULL, or_sworker, &jobs[t]);
+	for(int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+}
+
 /* ---------- MD5 of many equal-length buffers (threaded; hashing baseline) ---------- */
 typedef struct { const uint8_t* base; size_t stride, len; const size_t* lens; uint64_t pad; unsigned n, nt, tid; uint8_t* md5; uint32_t* crc; } or_hjob;
 static void* or_hworker(void* arg) {

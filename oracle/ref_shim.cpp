@@ -16,10 +16,16 @@ extern "C" {
 }
 #include "hasher/hasher.h"
 
+#include <atomic>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
+#if defined(__aarch64__) && defined(__linux__)
+#include <sys/auxv.h>
+#endif
 
 static std::string g_method_name;
 
@@ -136,6 +142,101 @@ void ref_md5multi(const uint8_t* const* bufs, unsigned n, size_t len, uint8_t* m
 	m.update((const void* const*)bufs, len);
 	m.end();
 	m.get(md5s);
+}
+
+// One whole create job the way ParPar runs it on the CPU: the GF
+// multiply-accumulate of every input into every recovery slice through
+// PAR2Proc + PAR2ProcCPU (GF16_AUTO, `threads` workers, or the controller's
+// own hardware_concurrency() default when threads <= 0,
+// gf16/controller_cpu.cpp:52-55), and, concurrently, the input hashes of
+// every file on a thread of its own, as each JS HasherInput object owns one
+// (src/gf.cc:926-954, 1015-1039): per-slice MD5+CRC32 (IFSC, last slice
+// zero-padded) and the file MD5.
+//   inputs: numIn rows `pitch` bytes apart, row i holding lens[i] bytes;
+//   file f: fileLens[f] bytes in the rows from firstRow[f];
+//   out: numRec rows of sliceSize bytes; valid[r] the checksum verdicts;
+//   ifsc: 20 bytes per row; fileMd5: 16 bytes per file;
+//   times[0] = wall seconds of the whole job (both parts), times[1] = GF part
+//   (first addInput to endInput completion), times[2] = hashing part.
+int ref_job(const uint8_t* inputs, size_t pitch, const size_t* lens, const uint16_t* inputNums, unsigned numIn,
+            size_t sliceSize, const uint16_t* exps, unsigned numRec, uint8_t* out, int* valid,
+            const uint64_t* fileLens, const uint32_t* firstRow, unsigned numFiles, uint8_t* ifsc, uint8_t* fileMd5,
+            int threads, double* times) {
+	setup_hasher();
+	PAR2Proc proc;
+	PAR2ProcCPU cpu(2);
+	if(threads > 0) cpu.setNumThreads(threads);
+	if(!proc.init(sliceSize, {{&cpu, 0, sliceSize}})) return -1;
+	if(!cpu.init(GF16_AUTO, 0)) return -2;
+	g_method_name = cpu.getMethodName();
+	if(!proc.setRecoverySlices(numRec, exps)) return -3;
+
+	auto hashFile = [&](unsigned f) {
+		IHasherInput* h = HasherInput_Create();
+		uint64_t left = fileLens[f];
+		size_t row = firstRow[f];
+		uint8_t* entry = ifsc + 20 * row;
+		while(left) {
+			size_t n = left < sliceSize ? (size_t)left : sliceSize;
+			h->update(inputs + row * pitch, n);
+			h->getBlock(entry, sliceSize - n);
+			entry += 20;
+			row++;
+			left -= n;
+		}
+		h->end(fileMd5 + 16 * f);
+		h->destroy();
+	};
+
+	auto t0 = std::chrono::steady_clock::now();
+	std::atomic<double> tHash(0.0);
+	std::vector<std::thread> hashers;
+	hashers.reserve(numFiles);
+	std::atomic<unsigned> hashersLeft(numFiles);
+	for(unsigned f = 0; f < numFiles; f++)
+		hashers.emplace_back([&, f]() {
+			hashFile(f);
+			if(hashersLeft.fetch_sub(1) == 1)
+				tHash = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+		});
+	std::vector<std::future<void>> pending;
+	pending.reserve(numIn);
+	for(unsigned i = 0; i < numIn; i++) {
+		proc.waitForAdd();
+		pending.push_back(proc.addInput(inputs + (size_t)i * pitch, lens[i], inputNums[i], false));
+	}
+	proc.endInput().get();
+	for(auto& f : pending) f.get();
+	double tGf = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+	for(auto& t : hashers) t.join();
+	double tAll = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+	for(unsigned r = 0; r < numRec; r++)
+		valid[r] = proc.getOutput(r, out + (size_t)r * sliceSize).get() ? 1 : 0;
+	proc.deinit();
+	if(times) { times[0] = tAll; times[1] = tGf; times[2] = tHash; }
+	return 0;
+}
+
+// The GF method GF16_AUTO resolves to on this host for `threads` workers,
+// the worker count, and the CPU features the reference's dispatch reads
+// (on aarch64: HWCAP ASIMD/PMULL/CRC32, HWCAP2 SVE2, HWCAP SVE), as text.
+int ref_host_info(char* buf, size_t len) {
+	PAR2ProcCPU cpu(1);
+	cpu.setSliceSize(65536);
+	if(!cpu.init(GF16_AUTO, 0)) return -1;
+	std::string caps;
+#if defined(__aarch64__) && defined(__linux__)
+	unsigned long hw = getauxval(AT_HWCAP), hw2 = getauxval(AT_HWCAP2);
+	char tmp[160];
+	snprintf(tmp, sizeof(tmp), "hwcap=0x%lx hwcap2=0x%lx asimd=%d pmull=%d crc32=%d sve=%d sve2=%d", hw, hw2,
+	         (int)((hw >> 1) & 1), (int)((hw >> 4) & 1), (int)((hw >> 7) & 1), (int)((hw >> 22) & 1), (int)((hw2 >> 1) & 1));
+	caps = tmp;
+#else
+	caps = "x86";
+#endif
+	snprintf(buf, len, "method=%s;threads=%d;%s", cpu.getMethodName(), cpu.getNumThreads(), caps.c_str());
+	cpu.deinit();
+	return 0;
 }
 
 } // extern "C"

@@ -197,7 +197,10 @@ int Engine::set_slice_size(size_t s) {
 }
 
 int Engine::set_current_slice_size(size_t s) {
-	if(s < 2 || (s & 1)) { set_error("slice size %zu must be even and >= 2", s); return -1; }
+	// 0: PAR2Proc gives this backend no bytes of a short last window when it
+	// splits slices over several backends (gf16/controller.cpp:100-112); it
+	// then adds nothing to it, and the CPU backend accepts the size as well
+	if(s && (s < 2 || (s & 1))) { set_error("slice size %zu must be even and >= 2", s); return -1; }
 	wait_idle();
 	currentSliceSize = s;
 	if(s > allocSliceSize) {

@@ -21,6 +21,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from .layout import file_layout  # noqa: F401  (re-exported)
 
 
 def par2_coefficients(input_nums, exps) -> np.ndarray:
@@ -66,19 +67,6 @@ def _input_log(L, i):
         log[exp] = np.arange(65535)
         _LOGS = np.array([log[L.par2cuda_coeff(k, 1)] for k in range(32768)], dtype=np.int64)
     return int(_LOGS[i])
-
-
-def file_layout(file_lens, S):
-    """(first_row[f], rows per file, per-row byte lengths) for files laid out as slices of S bytes."""
-    first, lens = [], []
-    r = 0
-    for ln in file_lens:
-        first.append(r)
-        n = max(1, (int(ln) + S - 1) // S)
-        for k in range(n):
-            lens.append(int(min(S, ln - k * S)) if ln else 0)
-        r += n
-    return np.array(first, dtype=np.uint32), np.array(lens, dtype=np.uint32)
 
 
 class ResidentJob:

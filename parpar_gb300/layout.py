@@ -1,0 +1,23 @@
+"""Slice layout of files (pure host code, no device library).
+
+PAR2 cuts every file into slices of the set's slice size, the last one
+shorter and zero-padded (lib/par2.js PAR2File, lib/par2gen.js:1198-1285);
+input slices are numbered in file order.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def file_layout(file_lens, S):
+    """(first_row[f], per-row byte lengths) for files laid out as slices of S bytes;
+    an empty file still takes one (empty) row."""
+    first, lens = [], []
+    r = 0
+    for ln in file_lens:
+        first.append(r)
+        n = max(1, (int(ln) + S - 1) // S)
+        for k in range(n):
+            lens.append(int(min(S, ln - k * S)) if ln else 0)
+        r += n
+    return np.array(first, dtype=np.uint32), np.array(lens, dtype=np.uint32)

@@ -5,7 +5,7 @@ with oracle/ref.mk (the reference's gf16/ + hasher/ sources compiled in place)
 and records its outputs on seeded synthetic inputs (parpar_gb300.synth), so the
 oracle restatement and the CUDA path can be checked against them anywhere.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    PARPAR_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -14,7 +14,6 @@ import ctypes
 import hashlib
 import json
 import os
-import subprocess
 import sys
 
 import numpy as np
@@ -72,9 +71,14 @@ def case_inputs(seed, n, S, ragged):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference checkout (default: $PARPAR_REFERENCE)")
     args = ap.parse_args()
-    subprocess.check_call(["make", "-s", "-f", "oracle/ref.mk", "REF=" + args.ref, "-j8"], cwd=ROOT)
+    from oracle import refsrc
+    if not refsrc.stage(args.ref):
+        sys.exit("no reference tree: pass --ref or set PARPAR_REFERENCE")
+    res = refsrc.build(with_cuda=False)
+    if res["error"]:
+        sys.exit(res["error"])
     R = O.ref()
     out = {"generator": "tests/golden/make_golden.py", "reference": "ParPar gf16/ + hasher/ (compiled by oracle/ref.mk)",
            "coeffs": [], "recovery": [], "cksum": [], "hash": [], "md5multi": []}
