@@ -236,11 +236,25 @@ int par2cuda_file_md5(const void* d_rows, size_t pitch_bytes, unsigned num_files
  * results.  No counterpart in the reference. */
 int par2cuda_file_md5_packed(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
                              const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, void* stream);
+/* par2cuda_file_md5 with `files_per_block` files (1, or a multiple of 32 up to
+ * 512) per block: the file MD5 chains of several jobs in flight (the rows of
+ * all of them reachable from d_rows through d_first_row) held on as few SMs as
+ * possible, so that the other SMs stay free for the jobs' contractions.  Same
+ * results.  No counterpart in the reference. */
+int par2cuda_file_md5_pooled(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
+                             const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, unsigned files_per_block,
+                             void* stream);
 /* MD5 of (d_prefix[i*prefix_len .. +prefix_len) ++ first data_len bytes of
  * row i) for each row: the recovery-packet hash that MD5Multi computes
  * (src/gf.cc:1075-1219, lib/par2.js:243-335).  One GPU thread per row. */
 int par2cuda_rows_md5(const void* d_rows, size_t pitch_bytes, unsigned num_rows, size_t data_len,
                       const uint8_t* d_prefix, unsigned prefix_len, uint8_t* d_md5, void* stream);
+/* Copies num_rows rows of row_bytes bytes between host and device memory (or
+ * within either) with one 2-D copy on `stream`: the H2D of input slices into
+ * the backend's pitched rows, the D2H of recovery rows into packed host
+ * slices.  Asynchronous with respect to the host for pinned host memory. */
+int par2cuda_copy_rows(void* dst, size_t dst_pitch, const void* src, size_t src_pitch, size_t row_bytes,
+                       unsigned num_rows, void* stream);
 /* Seeded synthetic bytes (same bytes as parpar_gb300/synth.py). */
 int par2cuda_synth_fill(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes,
                         uint64_t seed, uint64_t first_index, void* stream);

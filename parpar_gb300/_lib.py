@@ -92,6 +92,8 @@ SIGNATURES = [
     ("par2cuda_slice_hash", _i, [_vp, _sz, _u, _vp, _sz, _vp, _vp]),
     ("par2cuda_file_md5", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _vp]),
     ("par2cuda_file_md5_packed", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _vp]),
+    ("par2cuda_file_md5_pooled", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _u, _vp]),
+    ("par2cuda_copy_rows", _i, [_vp, _sz, _vp, _sz, _sz, _u, _vp]),
     ("par2cuda_rows_md5", _i, [_vp, _sz, _u, _sz, _vp, _u, _vp, _vp]),
     ("par2cuda_synth_fill", _i, [_vp, _sz, _u, _sz, _u64, _u64, _vp]),
     ("par2cuda_synth_fill_at", _i, [_vp, _sz, _u, _sz, _u64, _u64, _u64, _vp]),

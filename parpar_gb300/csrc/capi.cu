@@ -200,7 +200,13 @@ int par2cuda_file_md5(const void* d_rows, size_t pitch_bytes, unsigned num_files
 int par2cuda_file_md5_packed(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
                              const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, void* stream) {
 	return p2c::file_md5(d_rows, pitch_bytes, num_files, d_file_len, d_first_row, slice_bytes, d_md5, (cudaStream_t)stream,
-	                     true);
+	                     32);
+}
+int par2cuda_file_md5_pooled(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
+                             const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, unsigned files_per_block,
+                             void* stream) {
+	return p2c::file_md5(d_rows, pitch_bytes, num_files, d_file_len, d_first_row, slice_bytes, d_md5, (cudaStream_t)stream,
+	                     files_per_block);
 }
 int par2cuda_rows_md5(const void* d_rows, size_t pitch_bytes, unsigned num_rows, size_t data_len,
                       const uint8_t* d_prefix, unsigned prefix_len, uint8_t* d_md5, void* stream) {
@@ -215,6 +221,19 @@ int par2cuda_synth_fill(void* d_dst, size_t pitch_bytes, unsigned num_rows, size
 int par2cuda_synth_fill_at(void* d_dst, size_t pitch_bytes, unsigned num_rows, size_t row_bytes, uint64_t seed,
                            uint64_t first_index, uint64_t byte_offset, void* stream) {
 	return p2c::synth_fill(d_dst, pitch_bytes, num_rows, row_bytes, seed, first_index, (cudaStream_t)stream, byte_offset);
+}
+
+int par2cuda_copy_rows(void* dst, size_t dst_pitch, const void* src, size_t src_pitch, size_t row_bytes,
+                       unsigned num_rows, void* stream) {
+	if(!num_rows || !row_bytes) return 0;
+	if(!dst || !src || dst_pitch < row_bytes || src_pitch < row_bytes) {
+		p2c::set_error("copy_rows: null pointer or pitch below the row size");
+		return -1;
+	}
+	cudaError_t e = cudaMemcpy2DAsync(dst, dst_pitch, src, src_pitch, row_bytes, num_rows, cudaMemcpyDefault,
+	                                  (cudaStream_t)stream);
+	if(e != cudaSuccess) { p2c::set_error("cudaMemcpy2DAsync: %s", cudaGetErrorString(e)); return -1; }
+	return 0;
 }
 
 size_t par2cuda_coeff_index_bytes(unsigned num_rec, unsigned num_in) { return p2c::idx_bytes(num_rec, num_in); }

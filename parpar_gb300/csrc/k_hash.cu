@@ -280,9 +280,10 @@ int md5_chain_rate(double* bytesPerSec, cudaStream_t st) {
 // ---- per-file MD5 -----------------------------------------------------------
 // file f = rows first[f] .. first[f]+ceil(len[f]/sliceBytes)-1, each row
 // contributing sliceBytes bytes except the last.  One thread per file.
-__global__ void __launch_bounds__(32) k_file_md5(const uint8_t* rows, size_t pitch, unsigned nFiles,
-                                                 const uint64_t* fileLen, const uint32_t* firstRow,
-                                                 size_t sliceBytes, uint8_t* out)
+template<int MAXT>
+__global__ void __launch_bounds__(MAXT) k_file_md5(const uint8_t* rows, size_t pitch, unsigned nFiles,
+                                                   const uint64_t* fileLen, const uint32_t* firstRow,
+                                                   size_t sliceBytes, uint8_t* out)
 {
 	const unsigned f = blockIdx.x * blockDim.x + threadIdx.x;
 	if(f >= nFiles) return;
@@ -328,17 +329,31 @@ __global__ void __launch_bounds__(32) k_file_md5(const uint8_t* rows, size_t pit
 }
 
 int file_md5(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen, const uint32_t* dFirstRow,
-             size_t sliceBytes, uint8_t* dOut, cudaStream_t st, bool packed)
+             size_t sliceBytes, uint8_t* dOut, cudaStream_t st, unsigned filesPerBlock)
 {
 	if(!nFiles) return 0;
 	if(pitchBytes % 16) { set_error("row pitch must be a multiple of 16 bytes"); return -1; }
-	// one thread per file.  Default: one file per block, spread over SMs (the
-	// fastest chains: 108 MB/s).  Packed: 32 files per warp, ~6 % slower per
-	// chain but ceil(nFiles/32) blocks instead of nFiles, each of which keeps a
-	// full-register-file CTA of other work off its SM while the chains run.
-	const unsigned lanes = packed ? 32u : 1u;
-	k_file_md5<<<(nFiles + lanes - 1) / lanes, lanes, 0, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen,
-	                                                          dFirstRow, sliceBytes, dOut);
+	// one thread per file.  filesPerBlock 1 (default): one file per block,
+	// spread over SMs (the fastest chains: 108 MB/s).  32: one warp of files
+	// per block, ~6 % slower per chain but ceil(nFiles/32) blocks instead of
+	// nFiles, each of which keeps a full-register-file CTA of other work off
+	// its SM while the chains run.  Up to 512: the files of several jobs on
+	// as few SMs as possible (a warp issues one instruction per ~4-cycle
+	// dependency step, so a few warps per scheduler do not slow each other).
+	if(filesPerBlock == 1) {
+		k_file_md5<32><<<nFiles, 1, 0, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen, dFirstRow, sliceBytes, dOut);
+	} else if(filesPerBlock == 32) {
+		k_file_md5<32><<<(nFiles + 31) / 32, 32, 0, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen, dFirstRow,
+		                                                   sliceBytes, dOut);
+	} else {
+		if(filesPerBlock % 32 || filesPerBlock > 512) {
+			set_error("files per block %u must be 1 or a multiple of 32 up to 512", filesPerBlock);
+			return -1;
+		}
+		const unsigned per = min(filesPerBlock, (nFiles + 31) / 32 * 32);
+		k_file_md5<512><<<(nFiles + per - 1) / per, per, 0, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen,
+		                                                             dFirstRow, sliceBytes, dOut);
+	}
 	P2C_CUDA_TRY(cudaGetLastError());
 	return 0;
 }

@@ -66,7 +66,7 @@ int slice_hash(const void* rows, size_t pitchBytes, unsigned n, const uint32_t* 
                uint8_t* dOut, cudaStream_t st);
 // per-file MD5; file f spans consecutive rows from dFirstRow[f], dFileLen[f] bytes
 int file_md5(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen, const uint32_t* dFirstRow,
-             size_t sliceBytes, uint8_t* dOut, cudaStream_t st, bool packed = false);
+             size_t sliceBytes, uint8_t* dOut, cudaStream_t st, unsigned filesPerBlock = 1);
 // MD5 of (prefix[i] ++ row i's first dataLen bytes)
 int rows_md5(const void* rows, size_t pitchBytes, unsigned n, size_t dataLen, const uint8_t* dPrefix, unsigned prefixLen,
              uint8_t* dOut, cudaStream_t st);
