@@ -1,18 +1,27 @@
 """Benchmark: PAR2 recovery generation on one GB300 vs the reference's CPU path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload bandwidth|dense|plain|batched|serving] [--no-e2e] [--no-cpu-baseline]
+                    [--workload bandwidth|dense|plain|batched|serving|create] [--slots S] [--group G]
+                    [--no-e2e] [--no-cpu-baseline] [--no-dense]
 
 Workload (default "bandwidth", the configuration the metric is quoted on):
 2000 input slices x 2 MiB (40 files of seeded uneven lengths; the last slice of
 each file zero-padded), 200 recovery slices (exponents 0..199), with the
-per-slice MD5+CRC32 (IFSC) and per-file MD5 hashes, single read pass.  One
-step = one whole job.  Inputs are seeded synthetic data (parpar_gb300.synth).
+per-slice MD5+CRC32 (IFSC) and per-file MD5 hashes, single read pass.  Inputs
+are seeded synthetic data (parpar_gb300.synth).
 
-value: GF16 mul-adds/s with the inputs resident in HBM (device-timed with CUDA
-events).  e2e: the same job through the C ABI with pinned host buffers, the
-input H2D and result D2H inside the timed region.  --impl reference times the
-reference algorithm's CPU implementation on this host's cores.
+One step = one whole job.  The GPU arm streams K jobs through S resident slots
+(parpar_gb300.stream.JobStream: each job's contraction, checksums and IFSC, and
+the file MD5 chains of G jobs pooled into one launch), so that the serial MD5
+chain of one job's largest file overlaps other jobs' contractions; the timed
+region holds every kernel of all K jobs, and each job's latency is reported
+(p50/p99).  `single_job` gives one job at a time.  value: GF16 mul-adds/s with
+the inputs resident in HBM (CUDA events).  e2e: the same stream with every
+job's slices copied from pinned host memory and its results copied back.
+`dense`: the 4096 x 4096 x 256 KiB contraction.  --impl reference runs the
+reference's own CPU implementation (ParPar's PAR2ProcCPU with GF16_AUTO and its
+HasherInput per file, compiled on this host from staged sources) one whole job
+per step, on the same config.
 """
 from __future__ import annotations
 
@@ -29,6 +38,8 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+
+from parpar_gb300.layout import file_lengths  # noqa: E402  (pure host code, no device library)
 
 METRIC = "GF16 mul-adds/s"
 UNIT = "mul-adds/s"
@@ -70,22 +81,6 @@ WORKLOADS = {
                     desc="64 PAR2 jobs: N log-uniform [10,5000], S uniform 64 KiB..8 MiB (4-byte steps), R 1-30% of N; "
                          "byte-window passes under a 64 GiB HBM budget; persistent graph-captured comb launches vs per-job launches"),
 }
-
-
-def file_lengths(N, files, S, seed):
-    """Seeded uneven file lengths with sum(ceil(len/S)) == N, last slice partial."""
-    rng = np.random.default_rng(seed)
-    if files == 1:
-        return [N * S]
-    w = rng.uniform(0.5, 1.5, size=files)
-    counts = np.maximum(1, np.floor(w / w.sum() * N)).astype(int)
-    while counts.sum() < N:
-        counts[rng.integers(files)] += 1
-    while counts.sum() > N:
-        k = int(np.argmax(counts))
-        counts[k] -= 1
-    tails = rng.integers(1, S + 1, size=files)
-    return [int((c - 1) * S + t) for c, t in zip(counts, tails)]
 
 
 def sample_clocks(stop, out):
@@ -183,41 +178,28 @@ class CpuJob:
 
 
 def reference_core():
-    """The reference's own CPU core compiled on this host (oracle/_ref), or
-    None and the reason it is not there."""
-    import ctypes
+    """True when the reference's own CPU core is compiled on this host
+    (oracle/_ref), else False and the reason it is not there."""
     from oracle import refsrc
     if not os.path.exists(refsrc.REF_LIB):
         err = os.path.join(refsrc.REF_OUT, "build_error.txt")
         why = open(err).read().strip().splitlines()[0] if os.path.exists(err) else \
             "reference sources not staged on this host (oracle/_ref/src)"
-        return None, why
-    L = ctypes.CDLL(refsrc.REF_LIB)
-    vp, sz, u = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint
-    L.ref_job.restype = ctypes.c_int
-    L.ref_job.argtypes = [vp, sz, vp, vp, u, sz, vp, u, vp, vp, vp, vp, u, vp, vp, ctypes.c_int,
-                          ctypes.POINTER(ctypes.c_double)]
-    L.ref_host_info.restype = ctypes.c_int
-    L.ref_host_info.argtypes = [ctypes.c_char_p, sz]
-    L.ref_last_method_name.restype = ctypes.c_char_p
-    return L, None
+        return False, why
+    return True, None
 
 
-def _reference_step(L, job, threads):
+def _reference_step(job, threads):
     """One whole job through ParPar's PAR2Proc + PAR2ProcCPU (GF16_AUTO) with
     its HasherInput per file concurrently (oracle/ref_shim.cpp ref_job);
     returns (wall, gf, hash) seconds."""
-    import ctypes
-    from oracle.oracle import _p
-    t = (ctypes.c_double * 3)()
+    from oracle import oracle as O
     nf = len(job.file_lens) if job.hashes else 0
-    rc = L.ref_job(_p(job.x), job.S, _p(job.lens), _p(job.nums), job.N, job.S, _p(job.exps), job.R, _p(job.out),
-                   _p(job.valid), _p(job.file_lens), _p(job.first_row), nf, _p(job.ifsc), _p(job.fmd5), threads, t)
-    if rc != 0:
-        raise RuntimeError("reference job failed: %d" % rc)
-    if not job.valid.all():
+    out, valid, _, _, t = O.ref_job(job.x, job.lens, job.nums, job.exps, job.file_lens[:nf] if nf else None,
+                                    job.first_row[:nf] if nf else None, threads)
+    if not valid.all():
         raise RuntimeError("reference checksum verdict false")
-    return t[0], t[1], t[2]
+    return t
 
 
 def _port_step(job, threads):
@@ -259,17 +241,18 @@ def cpu_step_fn(threads):
     """(step function(job) -> (wall, gf, hash) seconds, description dict) of the
     best available CPU path: the reference's own core where it built on this
     host, else the oracle's port of its automatic method."""
-    L, why = reference_core()
-    if L is not None:
+    have, why = reference_core()
+    if have:
         import ctypes
+        from oracle import oracle as O
         buf = ctypes.create_string_buffer(512)
-        L.ref_host_info(buf, 512)
+        O.ref().ref_host_info(buf, 512)
         info = dict(kv.split("=", 1) for kv in buf.value.decode().split(";") if "=" in kv)
         host = buf.value.decode().split(";")[-1]
         desc = {"kind": "reference", "cores": threads,
                 "method": "ParPar PAR2ProcCPU, GF16_AUTO -> %s, %d threads; HasherInput per file (%s)"
                           % (info.get("method", "?"), threads, host)}
-        return (lambda job: _reference_step(L, job, threads)), desc
+        return (lambda job: _reference_step(job, threads)), desc
     desc = {"kind": "port", "cores": threads, "reference_unavailable": why}
 
     def step(job):
@@ -348,6 +331,276 @@ def bench_config(args, cfg, file_lens, world):
 
 
 # ---------------------------------------------------------------------------- GPU
+def single_job_measure(args, cfg, file_lens, job, steps, warmup, e2e=True):
+    """One job at a time on the resident job's rows (ResidentJob): `steps`
+    whole jobs back to back, each waiting for the previous one, timed with
+    CUDA events; returns ms per job, the contraction's and file MD5's device
+    times, and (e2e) the same job from pinned host buffers."""
+    import torch
+    from parpar_gb300 import _lib
+    L = _lib.load()
+    S, N, R = cfg["S"], cfg["N"], cfg["R"]
+    ev = []
+
+    def step(record=False):
+        cur = torch.cuda.current_stream(job.dev)
+        job.sa.wait_stream(cur)
+        job.sb.wait_stream(cur)
+        a, b = job.sa.cuda_stream, job.sb.cuda_stream
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if record else None
+        _lib.check(L.par2cuda_rows_checksum(job.d_in.data_ptr(), job.pw, N, job.d_lens.data_ptr(), S, 0, None,
+                                           job.d_ck.data_ptr(), a), "cksum")
+        if cfg["hashes"]:
+            if record:
+                e[2].record(job.sb)
+            _lib.check(L.par2cuda_file_md5(job.d_in.data_ptr(), job.pitch, len(file_lens), job.d_flen.data_ptr(),
+                                          job.d_first.data_ptr(), S, job.d_fmd5.data_ptr(), b), "file_md5")
+            if record:
+                e[3].record(job.sb)
+        if record:
+            e[0].record(job.sa)
+        _lib.check(L.par2cuda_muladd(job.d_in.data_ptr(), job.pw, N, job.d_coeff.data_ptr(), job.d_rec.data_ptr(),
+                                    job.pw, R, job.row_words, 0, job.method, job.d_scratch.data_ptr(),
+                                    job.scratch_bytes, a), "muladd")
+        if record:
+            e[1].record(job.sa)
+        _lib.check(L.par2cuda_rows_checksum(job.d_rec.data_ptr(), job.pw, R, None, S, 1, job.d_flags.data_ptr(),
+                                           job.d_ck.data_ptr(), a), "verify")
+        if cfg["hashes"]:
+            _lib.check(L.par2cuda_slice_hash(job.d_in.data_ptr(), job.pitch, N, job.d_lens.data_ptr(), S,
+                                            job.d_ifsc.data_ptr(), a), "slice_hash")
+        cur.wait_stream(job.sa)
+        cur.wait_stream(job.sb)
+        if record:
+            ev.append(e)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(steps):
+        step(record=True)
+    t1.record()
+    torch.cuda.synchronize()
+    if int(job.d_flags.sum()) != R:
+        raise RuntimeError("recovery checksum verification failed")
+    out = {"ms_per_job": t0.elapsed_time(t1) / steps, "jobs": steps,
+           "muladd_ms": float(np.mean([e[0].elapsed_time(e[1]) for e in ev])),
+           "file_md5_ms": float(np.mean([e[2].elapsed_time(e[3]) for e in ev])) if cfg["hashes"] else 0.0,
+           "launches_per_job": 6 + (2 if cfg["hashes"] else 0)}
+    out["value"] = N * R * (S // 2) / (out["ms_per_job"] / 1e3)
+    if e2e:
+        host_in = torch.empty((N, S), dtype=torch.uint8, pin_memory=True)
+        host_in.copy_(job.d_in.view(torch.uint8)[:, :S])
+        rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
+        torch.cuda.synchronize()
+        job.run_from_host(host_in, hashes=cfg["hashes"])
+        job.download(rec_host)
+        torch.cuda.synchronize()
+        t0.record()
+        for _ in range(steps):
+            job.run_from_host(host_in, hashes=cfg["hashes"])
+            _, _, _, flags = job.download(rec_host)
+        t1.record()
+        torch.cuda.synchronize()
+        if int(flags.sum()) != R:
+            raise RuntimeError("recovery checksum verification failed (e2e)")
+        ems = t0.elapsed_time(t1) / steps
+        out["e2e"] = {"value": N * R * (S // 2) / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": N * S,
+                      "d2h_bytes_per_step": job.d2h_bytes(), "ms_per_step": ems,
+                      "path": "par2cuda C ABI: pinned host slices -> H2D (per file, largest first, file MD5s starting "
+                              "as files land) -> job -> D2H recovery + IFSC + file MD5 + verdicts"}
+        del host_in, rec_host
+    return out
+
+
+def stream_measure(args, cfg, file_lens, local, rank, barrier, max_over_ranks):
+    """The job stream (parpar_gb300.stream.JobStream): args.steps jobs of the
+    workload, args.slots resident at once, file MD5s pooled per args.group
+    jobs; device-resident (value) and from pinned host buffers (e2e)."""
+    import torch
+    from parpar_gb300 import _lib
+    from parpar_gb300.stream import JobStream
+    S, N, R = cfg["S"], cfg["N"], cfg["R"]
+    js = JobStream(S, file_lens, list(range(R)), slots=args.slots, group=args.group, device=local,
+                   method=_lib.METHOD_NAMES[args.method], md5_block=args.md5_block)
+    js.fill_synthetic(seed0=1 + 1000 * rank)
+    torch.cuda.synchronize()
+    warm = max(args.warmup, args.group)
+    js.run(warm, first_job=0)
+    torch.cuda.synchronize()
+    js.clear_records()
+    launches0 = js.launches
+    barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    js.run(args.steps, first_job=warm, timing=True)
+    t1.record()
+    torch.cuda.synchronize()
+    barrier()
+    ms = max_over_ranks(t0.elapsed_time(t1) / args.steps)
+    used = min(js.slots, warm + args.steps)
+    if int(js.d_flags[:used].sum()) != used * R:
+        raise RuntimeError("recovery checksum verification failed in the job stream")
+    lat = js.latencies()
+    out = {"ms": ms, "launches": js.launches - launches0, "muladd_ms": js.muladd_ms(),
+           "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+           "slots": js.slots, "group": js.group}
+    if not args.no_e2e:
+        host_in = [torch.empty((N, S), dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+        for k, h in enumerate(host_in):
+            h.copy_(js.d_in.view(torch.uint8)[k * N:(k + 1) * N, :S])
+        host_out = js.host_out_buffers(3)
+        torch.cuda.synchronize()
+        # the host->device copy rate of one job's inputs on its own
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        L = _lib.load()
+        cur = torch.cuda.current_stream()
+        c0.record()
+        _lib.check(L.par2cuda_copy_rows(js.d_in.data_ptr(), js.pitch, host_in[0].data_ptr(), S, S, N, cur.cuda_stream), "h2d")
+        c1.record()
+        torch.cuda.synchronize()
+        h2d_gbps = N * S / (c0.elapsed_time(c1) / 1e3) / 1e9
+        first = warm + args.steps
+        js.run(warm, first_job=first, host_in=host_in, host_out=host_out)
+        torch.cuda.synchronize()
+        js.clear_records()
+        barrier()
+        t0.record()
+        js.run(args.steps, first_job=first + warm, host_in=host_in, host_out=host_out, timing=True)
+        t1.record()
+        torch.cuda.synchronize()
+        barrier()
+        ems = max_over_ranks(t0.elapsed_time(t1) / args.steps)
+        if not all(int(o[3].sum()) == R for o in host_out):
+            raise RuntimeError("recovery checksum verification failed in the job stream (e2e)")
+        lat = js.latencies()
+        out["e2e"] = {"value": N * R * (S // 2) / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": N * S,
+                      "d2h_bytes_per_step": js.d2h_bytes(), "ms_per_step": ems,
+                      "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                      "h2d_GBps_one_job": h2d_gbps,
+                      "path": "par2cuda C ABI, job stream: per job one 2-D H2D of its slices from pinned host memory "
+                              "into its slot, the job's kernels, one D2H of recovery + IFSC + file MD5 + verdicts into "
+                              "pinned host buffers; %d slots, file MD5s pooled per %d jobs" % (js.slots, js.group)}
+        del host_in, host_out
+    del js
+    torch.cuda.empty_cache()
+    return out
+
+
+def dense_measure(args, local, steps):
+    """The 4096 x 4096 x 256 KiB contraction (configs' dense workload) inside
+    the default run: device-resident value with its integer-ALU roofline, and
+    e2e from pinned host buffers."""
+    import torch
+    from parpar_gb300 import _lib
+    from parpar_gb300.job import ResidentJob
+    cfg = WORKLOADS["dense"]
+    S, N, R = cfg["S"], cfg["N"], cfg["R"]
+    fl = [N * S]
+    job = ResidentJob(S, fl, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
+    job.fill_synthetic(seed=7)
+    torch.cuda.synchronize()
+    r = single_job_measure(args, cfg, fl, job, steps, warmup=3, e2e=not args.no_e2e)
+    del job
+    torch.cuda.empty_cache()
+    return r
+
+
+def plugin_measure(args, cfg, file_lens, local, steps):
+    """e2e through the reference-facing plugin boundary: the PAR2ProcCUDA
+    engine driven the way GfProc drives a backend (src/gf.cc AddSlice /
+    EndInput / GetOutputSlice) with pinned host slices; GF + internal checksum
+    only (the reference's plugin does not hash; hashing is HasherInput's job)."""
+    import torch
+    from parpar_gb300 import _lib
+    from parpar_gb300.gfproc import GfProc
+    from parpar_gb300.layout import file_layout
+    S, N, R = cfg["S"], cfg["N"], cfg["R"]
+    _, row_lens = file_layout(file_lens, S)
+    host_in = torch.empty((N, S), dtype=torch.uint8, pin_memory=True)
+    tmp = torch.empty((N, S), dtype=torch.uint8, device=torch.device("cuda", local))
+    _lib.check(_lib.load().par2cuda_synth_fill(tmp.data_ptr(), S, N, S, 1, 0,
+                                              torch.cuda.current_stream().cuda_stream), "synth")
+    host_in.copy_(tmp)
+    del tmp
+    rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
+    g = GfProc(S, method=args.method, device=local)
+    g.set_recovery_slices(list(range(R)))
+    L = _lib.load()
+    ctx = g._ctx
+    ptrs = [host_in[i].data_ptr() for i in range(N)]
+    lens_ = [int(x) for x in row_lens]
+    null_cb = _lib.DONE_FN()  # NULL: no completion callback
+
+    def plugin_pass():
+        # the calls a native adapter makes: discardOutput, waitForAdd +
+        # addInput per slice, endInput, getOutput per recovery slice
+        L.par2cuda_discard_output(ctx)
+        for i in range(N):
+            L.par2cuda_wait_for_add(ctx)
+            _lib.check(L.par2cuda_add_input(ctx, ptrs[i], lens_[i], i, 0, null_cb, None), "add")
+        _lib.check(L.par2cuda_end_input(ctx, null_cb, None), "end")
+        _lib.check(L.par2cuda_sync(ctx), "sync")
+        # outputs without a per-slice callback (a ctypes callback into Python
+        # costs ~57 us per slice, which is this harness's cost, not the
+        # library's); verdicts read once all copies are done
+        for r in range(R):
+            _lib.check(L.par2cuda_get_output(ctx, r, rec_host[r].data_ptr(), null_cb, None), "get")
+        _lib.check(L.par2cuda_sync(ctx), "sync")
+        return all(L.par2cuda_output_valid(ctx, r) == 1 for r in range(R))
+    for _ in range(3):
+        plugin_pass()
+    times = []
+    okp = True
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        okp = plugin_pass() and okp
+        times.append(time.perf_counter() - t0)
+    if not okp:
+        raise RuntimeError("plugin path checksum verdict failed")
+    inf = g.info()
+    g.close()
+    tp = float(np.median(times))
+    mul_adds = N * R * (S // 2)
+    return {"value": mul_adds / tp, "unit": UNIT, "h2d_bytes_per_step": int(row_lens.sum()),
+            "d2h_bytes_per_step": R * S, "ms_per_step": tp * 1e3, "steps": steps,
+            "ms_min_max": [min(times) * 1e3, max(times) * 1e3],
+            "spread": (max(times) - min(times)) / tp,
+            "spread_p10_p90": float(np.percentile(times, 90) - np.percentile(times, 10)) / tp,
+            "batch": inf["staging_size"], "staging_areas": inf["staging_count"], "method_desc": inf["method_desc"],
+            "path": "C ABI plugin calls from the host: wait_for_add + add_input x N (pinned host slices), "
+                    "end_input, get_output x R, verdicts by output_valid; GF multiply-accumulate + internal "
+                    "checksum, no hashing (the reference plugin does not hash); host wall clock, median of steps"}
+
+
+def roofline_gf(mul_adds, muladd_ms, lop3_ops, n_sm, sm_mhz, kname, alg_bytes):
+    """Integer-ALU roofline of the contraction: 2 three-input LOP3 per word
+    mul-add (16x16 GF(2) matrix, ~128 set bits, 32-way bit slicing) against the
+    LOP3 rate measured on this device (par2cuda_lop3_rate)."""
+    rate = mul_adds / (muladd_ms / 1e3)
+    out = {"bound": "int-alu", "kernel": kname, "achieved": 2 * rate / 1e12, "peak": lop3_ops / 1e12,
+           "unit": "Tops/s", "frac": 2 * rate / lop3_ops, "traffic": None, "alg_bytes": alg_bytes,
+           "peak_source": "measured: LOP3 calibration kernel k_lop3_rate on this GPU (%.1f lanes/SM/clk at %.0f MHz); "
+                          "nominal 128 lanes would be %.1f Tops/s"
+                          % (lop3_ops / n_sm / (sm_mhz * 1e6), sm_mhz, n_sm * 128 * sm_mhz * 1e6 / 1e12),
+           "mul_adds_per_s": rate, "muladd_ms": muladd_ms}
+    if kname in KERNEL_TRAFFIC:
+        # DRAM bytes per launch scaled from the ncu capture of the same kernel
+        # (profiles/): inputs are read once and recovery rows written once, so
+        # traffic grows with (N + R) x S
+        tb, ab, what = KERNEL_TRAFFIC[kname]
+        out["traffic"] = tb / ab * alg_bytes
+        out["traffic_source"] = "ncu dram__bytes_read+write of %s (%.1f MB for %.1f MB algorithmic), scaled by " \
+                                "(N+R)*S" % (what, tb / 1e6, ab / 1e6)
+    return out
+
+
 def run_ours(args, cfg, file_lens):
     import torch
     import torch.distributed as dist
@@ -371,59 +624,9 @@ def run_ours(args, cfg, file_lens):
 
     S, N, R = cfg["S"], cfg["N"], cfg["R"]
     mul_adds = N * R * (S // 2)
-    if args.comb_shape:
-        _lib.check(_lib.load().par2cuda_set_comb_shape(args.comb_shape), "set_comb_shape")
-    job = ResidentJob(S, file_lens, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
-    job.fill_synthetic(seed=1 + rank)
-    torch.cuda.synchronize()
-
-    # per-kernel events on the launching streams (comb kernel on A, file MD5 on B)
     L = _lib.load()
-    ev = []
-
-    def step(record=False):
-        h0 = h1 = None
-        cur = torch.cuda.current_stream(dev)
-        job.sa.wait_stream(cur)
-        job.sb.wait_stream(cur)
-        a, b = job.sa.cuda_stream, job.sb.cuda_stream
-        _lib.check(L.par2cuda_rows_checksum(job.d_in.data_ptr(), job.pw, N, job.d_lens.data_ptr(), S, 0, None,
-                                           job.d_ck.data_ptr(), a), "cksum")
-        if cfg["hashes"]:
-            # the file MD5s (long serial chains) start at once on B; they read
-            # only each file's own bytes
-            h0 = torch.cuda.Event(enable_timing=True) if record else None
-            h1 = torch.cuda.Event(enable_timing=True) if record else None
-            if record:
-                h0.record(job.sb)
-            _lib.check(L.par2cuda_file_md5(job.d_in.data_ptr(), job.pitch, len(file_lens), job.d_flen.data_ptr(),
-                                          job.d_first.data_ptr(), S, job.d_fmd5.data_ptr(), b), "file_md5")
-            if record:
-                h1.record(job.sb)
-        k0 = torch.cuda.Event(enable_timing=True) if record else None
-        k1 = torch.cuda.Event(enable_timing=True) if record else None
-        if record:
-            k0.record(job.sa)
-        _lib.check(L.par2cuda_muladd(job.d_in.data_ptr(), job.pw, N, job.d_coeff.data_ptr(), job.d_rec.data_ptr(),
-                                    job.pw, R, job.row_words, 0, job.method, job.d_scratch.data_ptr(),
-                                    job.scratch_bytes, a), "muladd")
-        if record:
-            k1.record(job.sa)
-        _lib.check(L.par2cuda_rows_checksum(job.d_rec.data_ptr(), job.pw, R, None, S, 1, job.d_flags.data_ptr(),
-                                           job.d_ck.data_ptr(), a), "verify")
-        if cfg["hashes"]:
-            _lib.check(L.par2cuda_slice_hash(job.d_in.data_ptr(), job.pitch, N, job.d_lens.data_ptr(), S,
-                                            job.d_ifsc.data_ptr(), a), "slice_hash")
-        cur.wait_stream(job.sa)
-        cur.wait_stream(job.sb)
-        if record:
-            ev.append((k0, k1, h0, h1))
-
-    launches_per_step = 6 + (2 if cfg["hashes"] else 0)  # cksum x2, coeff->idx, comb, verify x2 (+ slice hash, file md5)
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    assert int(job.d_flags.sum()) == R, "recovery checksum verification failed"
+    if args.comb_shape:
+        _lib.check(L.par2cuda_set_comb_shape(args.comb_shape), "set_comb_shape")
     # roofline denominators measured on this device: the LOP3 rate (integer-ALU
     # bound of the contraction) and one MD5 chain's rate on one thread (the
     # latency bound of the one-stream-per-thread hash kernels)
@@ -440,155 +643,40 @@ def run_ours(args, cfg, file_lens):
         th = threading.Thread(target=sample_clocks, args=(stop, clock_lines), daemon=True)
         th.start()
         time.sleep(0.5)
-    barrier()
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record()
-    for _ in range(args.steps):
-        step(record=True)
-    t1.record()
-    torch.cuda.synchronize()
-    barrier()
-    ms = t0.elapsed_time(t1) / args.steps
-    ms = max_over_ranks(ms)
-    comb_ms = float(np.mean([k0.elapsed_time(k1) for k0, k1, _, _ in ev]))
-    hash_ms = float(np.mean([h0.elapsed_time(h1) for _, _, h0, h1 in ev])) if cfg["hashes"] else 0.0
-    value = whole_job_value(mul_adds, ms, world)
 
-    # e2e: pinned host inputs -> H2D -> job -> D2H of every result, via the C ABI
-    e2e = None
-    if not args.no_e2e:
-        host_in = torch.empty((N, S), dtype=torch.uint8, pin_memory=True)
-        host_in.copy_(job.d_in.view(torch.uint8)[:, :S])
-        rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
-        torch.cuda.synchronize()
-        for _ in range(max(1, args.warmup // 2)):
-            job.run_from_host(host_in, hashes=cfg["hashes"])
-            job.download(rec_host)
-        torch.cuda.synchronize()
+    use_stream = cfg["hashes"] and args.slots > 1
+    single = None
+    if use_stream:
+        st = stream_measure(args, cfg, file_lens, local, rank, barrier, max_over_ranks)
+        ms, muladd_ms, e2e = st["ms"], st["muladd_ms"], st.get("e2e")
+        launches = st["launches"]
+        job = ResidentJob(S, file_lens, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
+        job.fill_synthetic(seed=1 + rank)
+        single = single_job_measure(args, cfg, file_lens, job, min(args.steps, 3), warmup=1, e2e=not args.no_e2e)
+        del job
+        torch.cuda.empty_cache()
+    else:
+        job = ResidentJob(S, file_lens, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
+        job.fill_synthetic(seed=1 + rank)
         barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(args.steps):
-            job.run_from_host(host_in, hashes=cfg["hashes"])
-            _, _, _, flags = job.download(rec_host)
-        e1.record()
-        torch.cuda.synchronize()
+        r = single_job_measure(args, cfg, file_lens, job, args.steps, warmup=args.warmup, e2e=not args.no_e2e)
         barrier()
-        ems = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-        assert int(flags.sum()) == R
-        e2e = {"value": mul_adds * world / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": N * S,
-               "d2h_bytes_per_step": job.d2h_bytes(), "ms_per_step": ems,
-               "path": "par2cuda C ABI: pinned host slices -> H2D (per file, largest first, file MD5s starting as "
-                       "files land) -> job -> D2H recovery + IFSC + file MD5 + verdicts"}
-    # e2e through the reference-facing plugin boundary: the PAR2ProcCUDA engine
-    # driven like GfProc (src/gf.cc AddSlice / EndInput / GetOutputSlice) with
-    # pinned host slices; GF + internal checksum only (the reference's plugin
-    # does not hash; hashing is HasherInput's job)
+        ms = max_over_ranks(r["ms_per_job"])
+        muladd_ms, e2e = r["muladd_ms"], r.get("e2e")
+        launches = r["launches_per_job"] * args.steps
+        st = None
+        del job
+        torch.cuda.empty_cache()
+    value = whole_job_value(mul_adds, ms, world)
+    if e2e is not None:
+        e2e["value"] = e2e["value"] * world
+
+    dense = None
+    if args.workload == "bandwidth" and not args.no_dense:
+        dense = dense_measure(args, local, min(args.steps, 10))
     e2e_plugin = None
     if not args.no_e2e and not args.no_plugin:
-        from parpar_gb300.gfproc import GfProc
-        from parpar_gb300.job import file_layout
-        _, row_lens = file_layout(file_lens, S)
-        g = GfProc(S, method=args.method, device=local)
-        g.set_recovery_slices(list(range(R)))
-        views = [host_in[i, : int(row_lens[i])] for i in range(N)]
-
-        L2 = _lib.load()
-        ctx = g._ctx
-        ptrs = [v.data_ptr() for v in views]
-        lens_ = [int(x) for x in row_lens]
-        null_cb = _lib.DONE_FN()  # NULL: no completion callback
-
-        def plugin_pass():
-            # the calls a native adapter makes: discardOutput, waitForAdd +
-            # addInput per slice, endInput, getOutput per recovery slice
-            L2.par2cuda_discard_output(ctx)
-            for i in range(N):
-                L2.par2cuda_wait_for_add(ctx)
-                _lib.check(L2.par2cuda_add_input(ctx, ptrs[i], lens_[i], i, 0, null_cb, None), "add")
-            _lib.check(L2.par2cuda_end_input(ctx, null_cb, None), "end")
-            _lib.check(L2.par2cuda_sync(ctx), "sync")
-            # outputs without a per-slice callback (a ctypes callback into Python
-            # costs ~57 us per slice, which is this harness's cost, not the
-            # library's); verdicts read once all copies are done
-            for r in range(R):
-                _lib.check(L2.par2cuda_get_output(ctx, r, rec_host[r].data_ptr(), null_cb, None), "get")
-            _lib.check(L2.par2cuda_sync(ctx), "sync")
-            return all(L2.par2cuda_output_valid(ctx, r) == 1 for r in range(R))
-        plugin_pass()
-        t0p = time.perf_counter()
-        okp = True
-        for _ in range(args.plugin_steps):
-            okp = plugin_pass() and okp
-        tp = (time.perf_counter() - t0p) / args.plugin_steps
-        assert okp, "plugin path checksum verdict failed"
-        inf = g.info()
-        g.close()
-        e2e_plugin = {"value": mul_adds * world / tp, "unit": UNIT, "h2d_bytes_per_step": int(row_lens.sum()),
-                      "d2h_bytes_per_step": R * S, "ms_per_step": tp * 1e3, "steps": args.plugin_steps,
-                      "batch": inf["staging_size"], "staging_areas": inf["staging_count"], "method_desc": inf["method_desc"],
-                      "path": "C ABI plugin calls from the host: wait_for_add + add_input x N (pinned host slices), "
-                              "end_input, get_output x R, verdicts by output_valid; GF multiply-accumulate + internal "
-                              "checksum, no hashing (the reference plugin does not hash); host wall clock"}
-    # several independent jobs in flight: job k runs its whole pass on its own
-    # context stream with its own seeded inputs, so one job's per-file MD5
-    # chains (serial, ~100 MB/s per GPU thread) overlap the others' work;
-    # each job's steps stay in order on its stream
-    inflight = None
-    if args.inflight > 1 and cfg["hashes"]:
-        jobs_k = [job] + [ResidentJob(S, file_lens, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
-                          for _ in range(args.inflight - 1)]
-        for k, jk in enumerate(jobs_k[1:], 1):
-            jk.fill_synthetic(seed=1 + rank + 1000 * k)
-        ctx = [torch.cuda.Stream(device=dev) for _ in jobs_k]
-        cur = torch.cuda.current_stream(dev)
-
-        def round_(upload=None, down=None):
-            for k, jk in enumerate(jobs_k):
-                ctx[k].wait_stream(cur)
-                with torch.cuda.stream(ctx[k]):
-                    if upload is not None:
-                        jk.upload(upload)
-                    jk.run(hashes=True, packed_md5=True)
-                    if down is not None:
-                        jk.download(down[k])
-            for c in ctx:
-                cur.wait_stream(c)
-        round_()
-        torch.cuda.synchronize()
-        i0 = torch.cuda.Event(enable_timing=True)
-        i1 = torch.cuda.Event(enable_timing=True)
-        i0.record()
-        for _ in range(args.steps):
-            round_()
-        i1.record()
-        torch.cuda.synchronize()
-        ims = max_over_ranks(i0.elapsed_time(i1) / args.steps)
-        assert all(int(jk.d_flags.sum()) == R for jk in jobs_k)
-        inflight = {"jobs_in_flight": len(jobs_k), "value": mul_adds * len(jobs_k) * world / (ims / 1e3), "unit": UNIT,
-                    "ms_per_round": ims, "jobs_per_s": len(jobs_k) * world / (ims / 1e3),
-                    "desc": "%d independent jobs of this workload (distinct seeded inputs, each resident) per round, "
-                            "each on its own stream; whole pass per job incl. IFSC + file MD5 (chains packed 32 per "
-                            "warp so that they leave the other SMs to the other jobs)" % len(jobs_k)}
-        if e2e is not None:
-            downs = [torch.empty((R, S), dtype=torch.uint8, pin_memory=True) for _ in jobs_k]
-            round_(host_in, downs)
-            torch.cuda.synchronize()
-            i0.record()
-            for _ in range(args.steps):
-                round_(host_in, downs)
-            i1.record()
-            torch.cuda.synchronize()
-            ems_k = max_over_ranks(i0.elapsed_time(i1) / args.steps)
-            inflight["e2e"] = {"value": mul_adds * len(jobs_k) * world / (ems_k / 1e3), "unit": UNIT,
-                               "ms_per_round": ems_k, "h2d_bytes_per_round": N * S * len(jobs_k),
-                               "d2h_bytes_per_round": job.d2h_bytes() * len(jobs_k)}
-            del downs
-        del jobs_k
-        torch.cuda.empty_cache()
+        e2e_plugin = plugin_measure(args, cfg, file_lens, local, args.plugin_steps)
 
     stop.set()
     if th:
@@ -603,62 +691,66 @@ def run_ours(args, cfg, file_lens):
     peaks = measured_peaks()
     sm_mhz = (clocks or {}).get("sm_mhz") or (peaks or {}).get("sm_max_mhz") or 2070.0
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
-    # int-ALU roofline of the contraction: 2 three-input LOP3 per word mul-add
-    # (16x16 GF(2) matrix, ~128 set bits, 32-way bit slicing) against the
-    # LOP3 rate measured on this device (par2cuda_lop3_rate)
-    alu_peak = lop3.value / 1e12
-    alu_nominal = n_sm * 128 * sm_mhz * 1e6 / 1e12
     kname = _lib.comb_kernel_name(L.par2cuda_comb_shape_for(R)) if args.method in ("comb", "auto") else \
         {"xor": "k_xor_muladd", "nibble": "k_nibble_muladd", "tensor": "k_tc_muladd"}[args.method]
-    comb_rate = mul_adds / (comb_ms / 1e3)
     alg_bytes = (N + R) * S  # read every input once, write every recovery once
     hbm_peak = (peaks or {}).get("hbm_gbs", 6800.0)
+    rgf = roofline_gf(mul_adds, muladd_ms, lop3.value, n_sm, sm_mhz, kname, alg_bytes)
+    if args.traffic_bytes:
+        rgf["traffic"] = args.traffic_bytes
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u16 GF(2^16)", "data": "synthetic (seeded splitmix64 slices), inputs resident in HBM",
         "config": bench_config(args, cfg, file_lens, world),
+        "step": ("one whole job of the workload; jobs stream through %d resident slots (file MD5 chains of %d jobs "
+                 "pooled in one launch, %d per block), the timed region holding every kernel of all %d jobs" %
+                 (args.slots, args.group, args.md5_block, args.steps)) if use_stream else "one whole job, jobs back to back",
         "src_GBps_x_recovery": N * S * R * world / (ms / 1e3) / 1e9,
-        "kernels_ms": {"muladd": comb_ms, "file_md5": hash_ms, "step": ms},
         "method": args.method,
-        "roofline_gf": {"bound": "int-alu", "kernel": kname, "achieved": 2 * comb_rate / 1e12,
-                     "peak": alu_peak, "unit": "Tops/s", "frac": 2 * comb_rate / 1e12 / alu_peak,
-                     "traffic": None, "alg_bytes": alg_bytes,
-                     "peak_source": "measured: LOP3 calibration kernel k_lop3_rate on this GPU (%.1f lanes/SM/clk at "
-                                    "%.0f MHz); nominal 128 lanes would be %.1f Tops/s" %
-                                    (lop3.value / n_sm / (sm_mhz * 1e6), sm_mhz, alu_nominal),
-                     "mul_adds_per_s": comb_rate},
-        "roofline_hbm": {"bound": "hbm", "kernel": kname, "achieved": alg_bytes / (comb_ms / 1e3) / 1e9,
-                         "peak": hbm_peak, "unit": "GB/s", "frac": alg_bytes / (comb_ms / 1e3) / 1e9 / hbm_peak,
+        "roofline_gf": rgf,
+        "roofline_hbm": {"bound": "hbm", "kernel": kname, "achieved": alg_bytes / (muladd_ms / 1e3) / 1e9,
+                         "peak": hbm_peak, "unit": "GB/s", "frac": alg_bytes / (muladd_ms / 1e3) / 1e9 / hbm_peak,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"},
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": launches,
         "clocks": clocks,
         "e2e": e2e,
         "e2e_plugin": e2e_plugin,
-        "inflight": inflight,
     }
-    if args.traffic_bytes:
-        line["roofline_gf"]["traffic"] = args.traffic_bytes
-    elif kname in KERNEL_TRAFFIC:
-        # DRAM bytes per launch scaled from the ncu capture of the same kernel
-        # (profiles/): inputs are read once and recovery rows written once, so
-        # traffic grows with (N + R) x S
-        tb, ab, what = KERNEL_TRAFFIC[kname]
-        line["roofline_gf"]["traffic"] = tb / ab * alg_bytes
-        line["roofline_gf"]["traffic_source"] = "ncu dram__bytes_read+write of %s (%.1f MB for %.1f MB algorithmic), " \
-            "scaled by (N+R)*S" % (what, tb / 1e6, ab / 1e6)
+    if st is not None:
+        line["p50_latency_s"] = st["p50_latency_s"]
+        line["p99_latency_s"] = st["p99_latency_s"]
+        line["latency_def"] = "per job: first kernel (its contraction side or its group's file MD5 launch) to last"
+        line["kernels_ms"] = {"muladd_in_stream": muladd_ms, "step": ms}
+    if single is not None:
+        line["single_job"] = {"value": single["value"], "ms_per_job": single["ms_per_job"],
+                              "muladd_ms": single["muladd_ms"], "file_md5_ms": single["file_md5_ms"],
+                              "e2e": single.get("e2e"),
+                              "desc": "one job in flight at a time: bound by the MD5 chain of its largest file "
+                                      "(%.0f MB) on one GPU thread" % (max(file_lens) / 1e6)}
     if cfg["hashes"]:
-        big = max(file_lens)
-        line["roofline_md5"] = {
-            "bound": "latency", "kernel": "k_file_md5", "achieved": big / (hash_ms / 1e3) / 1e6,
-            "peak": md5_chain.value / 1e6, "unit": "MB/s per GPU thread (largest file's chain)",
-            "frac": big / (hash_ms / 1e3) / md5_chain.value,
-            "traffic": MD5_TRAFFIC[0] / MD5_TRAFFIC[1] * sum(file_lens),
-            "traffic_source": "ncu dram__bytes_read+write of k_file_md5 on 4 files (%.1f MB for %.1f MB hashed), "
-                              "scaled by the bytes hashed" % (MD5_TRAFFIC[0] / 1e6, MD5_TRAFFIC[1] / 1e6),
-            "peak_source": "measured: k_md5_chain, one MD5 stream on one thread with its data in registers"}
-    # `roofline` is the kernel that bounds the step (the longest live kernel time)
-    line["roofline"] = dict(line["roofline_md5"] if cfg["hashes"] and hash_ms > comb_ms else line["roofline_gf"])
+        fm = single["file_md5_ms"] if single else None
+        if fm:
+            big = max(file_lens)
+            line["roofline_md5"] = {
+                "bound": "latency", "kernel": "k_file_md5", "achieved": big / (fm / 1e3) / 1e6,
+                "peak": md5_chain.value / 1e6, "unit": "MB/s per GPU thread (largest file's chain)",
+                "frac": big / (fm / 1e3) / md5_chain.value,
+                "traffic": MD5_TRAFFIC[0] / MD5_TRAFFIC[1] * sum(file_lens),
+                "traffic_source": "ncu dram__bytes_read+write of k_file_md5 on 4 files (%.1f MB for %.1f MB hashed), "
+                                  "scaled by the bytes hashed" % (MD5_TRAFFIC[0] / 1e6, MD5_TRAFFIC[1] / 1e6),
+                "peak_source": "measured: k_md5_chain, one MD5 stream on one thread with its data in registers"}
+    # `roofline`: the kernel that takes most of the timed region's device time
+    # (the contraction in the job stream and the dense workload)
+    line["roofline"] = dict(rgf)
+    if dense is not None:
+        dm = WORKLOADS["dense"]
+        d_mul = dm["N"] * dm["R"] * (dm["S"] // 2)
+        dk = _lib.comb_kernel_name(L.par2cuda_comb_shape_for(dm["R"])) if args.method in ("comb", "auto") else kname
+        line["dense"] = {"desc": dm["desc"], "value": dense["value"], "unit": UNIT, "ms_per_step": dense["ms_per_job"],
+                         "steps": dense["jobs"], "e2e": dense.get("e2e"),
+                         "roofline_gf": roofline_gf(d_mul, dense["muladd_ms"], lop3.value, n_sm, sm_mhz, dk,
+                                                    (dm["N"] + dm["R"]) * dm["S"])}
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1)
     print(json.dumps(line))
@@ -860,14 +952,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-plugin", action="store_true", help="skip the plugin-boundary e2e measurement")
-    ap.add_argument("--plugin-steps", type=int, default=2)
+    ap.add_argument("--plugin-steps", type=int, default=9)
     ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor"], default="comb",
                     help="multiply-accumulate kernel of the resident-job workloads")
     ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")
     ap.add_argument("--comb-shape", type=int, default=0,
                     help="pin the comb kernel's CTA shape (par2cuda_set_comb_shape; 0 = automatic)")
-    ap.add_argument("--inflight", type=int, default=8,
-                    help="independent jobs in flight for the multi-job figure of hashing workloads (0/1 = skip)")
+    ap.add_argument("--slots", type=int, default=24,
+                    help="jobs resident at once in the job stream of hashing workloads (1 = one job at a time)")
+    ap.add_argument("--group", type=int, default=8, help="jobs whose file MD5 chains share one launch in the job stream")
+    ap.add_argument("--md5-block", type=int, default=128, help="file MD5 chains per block in the job stream (32..512)")
+    ap.add_argument("--no-dense", action="store_true", help="skip the dense-contraction figure of the default run")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline_gf.traffic")
     args = ap.parse_args()

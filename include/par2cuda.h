@@ -189,6 +189,13 @@ int par2cuda_lop3_rate(double* ops_per_s, void* stream);
  * kernels: 1 when a bounded wait inside a kernel gave up (its results are then
  * invalid), 0 otherwise, negative if the flag could not be read. */
 int par2cuda_device_error(void);
+/* Self-test of the kernels' bounded waits (no counterpart in the reference):
+ * one warp waits, with the multiply-accumulate kernels' own wait helper and a
+ * limit of `polls` (1..2^22) polls, on an mbarrier that nothing arrives on.
+ * The wait gives up, sets the flag par2cuda_device_error() reports, and the
+ * kernel returns; *gave_up = 1 then, *seconds = the kernel's duration.  The
+ * context stays usable.  The kernels themselves use 2^22 polls. */
+int par2cuda_wait_selftest(unsigned polls, int* gave_up, double* seconds);
 /* Scratch bytes par2cuda_muladd needs for (num_rec, num_in). */
 size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in);
 /* rec[r][0..n_words) (^)= sum_i coeff[r*num_in + i] * in[i][0..n_words),
@@ -208,8 +215,11 @@ int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in
  * num_rec * ceil(num_in / 8) <= 262144 (larger calls are rejected with an
  * error; split the inputs over several calls with accumulate = 1).  It
  * allocates nothing.  The first call on a device looks up the array's address
- * (make it before any stream capture).  All calls share the array: calls that
- * overlap on the GPU race, so order them on one stream or with events. */
+ * (make it before any stream capture) and keeps it for the life of the
+ * process: do not use this entry point across a cudaDeviceReset or anything
+ * else that destroys and recreates the device's primary context, which can
+ * move the array.  All calls share the array: calls that overlap on the GPU
+ * race, so order them on one stream or with events. */
 int par2cuda_muladd_noalloc(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in,
                             const uint16_t* d_coeff, uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec,
                             size_t n_words, int accumulate, void* stream);

@@ -103,8 +103,40 @@ def ref():
         L.ref_crc32.restype = ctypes.c_uint32; L.ref_crc32.argtypes = [vp, sz]
         L.ref_md5crc.restype = ctypes.c_uint32; L.ref_md5crc.argtypes = [vp, sz, sz, vp]
         L.ref_md5multi.restype = None; L.ref_md5multi.argtypes = [vp, ctypes.c_uint, sz, vp]
+        L.ref_job.restype = i32
+        L.ref_job.argtypes = [vp, sz, vp, vp, ctypes.c_uint, sz, vp, ctypes.c_uint, vp, vp, vp, vp, ctypes.c_uint,
+                              vp, vp, i32, ctypes.POINTER(ctypes.c_double)]
+        L.ref_host_info.restype = i32
+        L.ref_host_info.argtypes = [ctypes.c_char_p, sz]
         _ref = L
     return _ref
+
+
+def ref_job(x: np.ndarray, lens, input_nums, exps, file_lens=None, first_rows=None, threads: int = 0):
+    """One whole create job through the reference's own CPU core
+    (oracle/ref_shim.cpp ref_job: PAR2Proc + PAR2ProcCPU with GF16_AUTO, and
+    HasherInput per file concurrently).  x: uint8 [n, S] rows, row i holding
+    lens[i] bytes.  Returns (recovery [r, S], valid [r], ifsc bytes, file MD5
+    bytes, (wall, gf, hash) seconds)."""
+    L = ref()
+    x = np.ascontiguousarray(x, dtype=np.uint8)
+    n, S = x.shape
+    lens = np.ascontiguousarray(lens, dtype=np.uint64)
+    nums = np.ascontiguousarray(input_nums, dtype=np.uint16)
+    e = np.ascontiguousarray(exps, dtype=np.uint16)
+    nf = 0 if file_lens is None else len(file_lens)
+    fl = np.ascontiguousarray(file_lens if nf else [0], dtype=np.uint64)
+    fr = np.ascontiguousarray(first_rows if nf else [0], dtype=np.uint32)
+    out = np.zeros((len(e), S), dtype=np.uint8)
+    valid = np.zeros(len(e), dtype=np.int32)
+    ifsc = np.zeros(max(n, 1) * 20, dtype=np.uint8)
+    fmd5 = np.zeros(max(nf, 1) * 16, dtype=np.uint8)
+    t = (ctypes.c_double * 3)()
+    rc = L.ref_job(_p(x), S, _p(lens), _p(nums), n, S, _p(e), len(e), _p(out), _p(valid), _p(fl), _p(fr), nf,
+                   _p(ifsc), _p(fmd5), threads, t)
+    if rc:
+        raise RuntimeError("reference job failed: %d" % rc)
+    return out, valid, ifsc[: n * 20].tobytes(), fmd5[: nf * 16].tobytes(), (t[0], t[1], t[2])
 
 
 def _p(a: np.ndarray):

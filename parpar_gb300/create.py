@@ -43,12 +43,22 @@ from .job import ResidentJob
 
 DEFAULT_CREATOR = "par2cuda (GB300 PAR2 recovery backend)"
 
+# Pinned host buffers (the ingest ring and the recovery download) are kept
+# for later calls: pinning hundreds of MB per call costs more than the work it
+# carries.  create() calls run one at a time (the buffers are shared);
+# release_pinned() frees them.
 _PINNED: dict = {}
+_CREATE_LOCK = threading.Lock()
+
+
+def release_pinned() -> None:
+    """Frees the pinned host buffers kept from earlier create() calls."""
+    with _CREATE_LOCK:
+        _PINNED.clear()
 
 
 def _pinned(key, rows: int, cols: int) -> torch.Tensor:
-    """A pinned host buffer of rows x cols bytes, kept for later calls:
-    pinning hundreds of MB per call costs more than the work it carries."""
+    """A pinned host buffer of rows x cols bytes, kept for later calls."""
     n = rows * cols
     t = _PINNED.get(key)
     if t is None or t.numel() < n:
@@ -221,7 +231,14 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
            names=None, device: int = 0, index: bool = True, stats: dict | None = None):
     """Creates the PAR2 set for `paths`; returns the written file names.
     `stats`, if given, receives the wall-clock time (s) at which each stage
-    ended, measured from the call (stages are synchronised to measure them)."""
+    ended, measured from the call (stages are synchronised to measure them).
+    Concurrent calls run one after the other.  Output files are written under
+    temporary names and renamed once complete; on an error none is left."""
+    with _CREATE_LOCK:
+        return _create(paths, slice_size, recovery_slices, out_base, creator, names, device, index, stats)
+
+
+def _create(paths, slice_size, recovery_slices, out_base, creator, names, device, index, stats):
     import time
     t0 = time.perf_counter()
 
@@ -313,9 +330,12 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
     rec_host.copy_(job.d_rec.view(torch.uint8)[:, :S])
     rec_np = rec_host.numpy()
 
+    def tmp_name(name):
+        return name + ".part"
+
     def write_recovery(item):
         name, total, lay = item
-        fd = os.open(name, os.O_WRONLY | os.O_CREAT | os.O_TRUNC, 0o644)
+        fd = os.open(tmp_name(name), os.O_WRONLY | os.O_CREAT | os.O_TRUNC, 0o644)
         try:
             os.ftruncate(fd, total)
             for pos, kind, k in lay:
@@ -327,26 +347,36 @@ def create(paths, slice_size: int, recovery_slices: int, out_base: str, creator:
         return name
 
     from concurrent.futures import ThreadPoolExecutor
-    with ThreadPoolExecutor(max_workers=min(8, len(layouts))) as ex:
-        written = list(ex.map(write_recovery, layouts))
-    mark("recovery written")
+    try:
+        with ThreadPoolExecutor(max_workers=min(8, len(layouts))) as ex:
+            written = list(ex.map(write_recovery, layouts))
+        mark("recovery written")
 
-    job.file_md5_finish()
-    torch.cuda.synchronize()
-    mark("file_md5")
-    fmd5 = job.d_fmd5.cpu().numpy().reshape(len(paths), 16)
-    crit = critical(lambda f: fmd5[f].tobytes())
-    if [len(c) for c in crit] != crit_len:
-        raise RuntimeError("critical packet sizes changed")
-    for name, total, lay in layouts:
-        fd = os.open(name, os.O_WRONLY)
-        try:
-            for pos, kind, k in lay:
-                if kind == "crit":
-                    os.pwrite(fd, crit[k], pos)
-                elif kind == "creator":
-                    os.pwrite(fd, creator_pkt, pos)
-        finally:
-            os.close(fd)
+        job.file_md5_finish()
+        torch.cuda.synchronize()
+        mark("file_md5")
+        fmd5 = job.d_fmd5.cpu().numpy().reshape(len(paths), 16)
+        crit = critical(lambda f: fmd5[f].tobytes())
+        if [len(c) for c in crit] != crit_len:
+            raise RuntimeError("critical packet sizes changed")
+        for name, total, lay in layouts:
+            fd = os.open(tmp_name(name), os.O_WRONLY)
+            try:
+                for pos, kind, k in lay:
+                    if kind == "crit":
+                        os.pwrite(fd, crit[k], pos)
+                    elif kind == "creator":
+                        os.pwrite(fd, creator_pkt, pos)
+            finally:
+                os.close(fd)
+        for name in written:
+            os.replace(tmp_name(name), name)
+    except BaseException:
+        for name, _, _ in layouts:
+            try:
+                os.remove(tmp_name(name))
+            except OSError:
+                pass
+        raise
     mark("written")
     return written

@@ -142,6 +142,11 @@ int par2cuda_lop3_rate(double* ops_per_s, void* stream) {
 	return p2c::lop3_rate(ops_per_s, (cudaStream_t)stream);
 }
 
+int par2cuda_wait_selftest(unsigned polls, int* gave_up, double* seconds) {
+	if(polls == 0 || polls > (1u << 22)) { p2c::set_error("wait self-test: polls must be 1..2^22"); return -1; }
+	return p2c::wait_selftest(polls, gave_up, seconds);
+}
+
 int par2cuda_device_error(void) {
 	int a = p2c::comb_error_take(), b = p2c::tc_error_take();
 	if(a < 0 || b < 0) return -1;

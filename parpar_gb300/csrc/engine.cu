@@ -88,6 +88,7 @@ void Engine::free_staging() {
 		if(a.dDesc) cudaFree(a.dDesc);
 		a.dIn = nullptr; a.hBounce = nullptr; a.hDesc = nullptr; a.dDesc = nullptr;
 		a.bounceBytes = 0;
+		a.descBytes = 0;
 	}
 	stagingPitch = 0;
 }
@@ -187,7 +188,14 @@ int Engine::init(int m, unsigned inputBatch) {
 	processingAdd = false;
 	for(auto& a : staging) a.active = false;
 	initialised = true;
-	return alloc_staging();
+	if(alloc_staging()) {
+		// leave nothing half-allocated: the backend refuses inputs until a
+		// later init succeeds
+		free_staging();
+		initialised = false;
+		return -1;
+	}
+	return 0;
 }
 
 int Engine::set_slice_size(size_t s) {
@@ -207,8 +215,16 @@ int Engine::set_current_slice_size(size_t s) {
 		// upsizing: reallocate (PAR2ProcCPU::setCurrentSliceSize, controller_cpu.cpp:147-168)
 		allocSliceSize = s;
 		sliceSize = std::max(sliceSize, s);
-		if(initialised && alloc_staging()) return -1;
-		if(!outputExponents.empty() && alloc_processing()) return -1;
+		if(initialised && alloc_staging()) {
+			free_staging();
+			initialised = false;
+			return -1;
+		}
+		if(!outputExponents.empty() && alloc_processing()) {
+			free_processing();
+			outputExponents.clear();
+			return -1;
+		}
 	}
 	return 0;
 }
@@ -219,8 +235,15 @@ int Engine::set_recovery_slices(unsigned n, const uint16_t* exps) {
 	if(exps) for(unsigned i = 0; i < n; i++) outputExponents[i] = exps[i];
 	if(!n) return 0;
 	if(!initialised) { set_error("init must be called before setRecoverySlices"); return -1; }
-	if(alloc_desc()) return -1;
-	return alloc_processing();
+	if(alloc_desc() || alloc_processing()) {
+		// the reference reports this as "Failed to allocate memory"; the
+		// backend then holds no recovery rows and refuses inputs until a
+		// later setRecoverySlices succeeds
+		free_processing();
+		outputExponents.clear();
+		return -1;
+	}
+	return 0;
 }
 
 // ------------------------------------------------------------------ adding

@@ -228,9 +228,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" :: "r"(smem_addr(bar)) : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit = P2C_WAIT_LIMIT) {
 	const unsigned a = smem_addr(bar);
-	for(unsigned i = 0; i < P2C_WAIT_LIMIT; i++) {
+	for(unsigned i = 0; i < limit; i++) {
 		unsigned ok;
 		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
 		             : "=r"(ok) : "r"(a), "r"(parity) : "memory");
@@ -238,6 +238,47 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
 	}
 	atomicExch(&g_comb_error, 1u);
 	return false;
+}
+
+// Self-test of the bounded wait: one warp waits on an mbarrier that nothing
+// arrives on, with the same helper as the kernels above and `polls` as its
+// limit; the wait gives up, records the error flag and the kernel returns.
+__device__ unsigned g_wait_selftest;
+__global__ void k_wait_selftest(unsigned polls) {
+	__shared__ __align__(8) uint64_t bar;
+	if(threadIdx.x == 0) mbar_init(&bar, 1);
+	__syncthreads();
+	const bool ok = mbar_wait(&bar, 0, polls);
+	if(threadIdx.x == 0) g_wait_selftest = ok ? 1u : 2u;
+}
+
+int wait_selftest(unsigned polls, int* gaveUp, double* seconds) {
+	cudaStream_t st;
+	P2C_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	const unsigned zero = 0;
+	cudaMemcpyToSymbolAsync(g_wait_selftest, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, st);
+	cudaEventRecord(e0, st);
+	k_wait_selftest<<<1, 32, 0, st>>>(polls);
+	cudaError_t le = cudaGetLastError();
+	cudaEventRecord(e1, st);
+	cudaError_t se = cudaStreamSynchronize(st);
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, e0, e1);
+	unsigned out = 0;
+	cudaMemcpyFromSymbol(&out, g_wait_selftest, sizeof(out));
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaStreamDestroy(st);
+	if(le != cudaSuccess || se != cudaSuccess) {
+		set_error("wait self-test: %s", cudaGetErrorString(le != cudaSuccess ? le : se));
+		return -1;
+	}
+	if(gaveUp) *gaveUp = out == 2 ? 1 : 0;
+	if(seconds) *seconds = ms * 1e-3;
+	return 0;
 }
 
 // WIDE = 1: each lane owns 4 words (LDS.64 per lookup, 128-word tiles,

@@ -82,4 +82,7 @@ int tc_error_take();
 int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, uint64_t seed, uint64_t first, cudaStream_t st,
                uint64_t byteOffset = 0);
 
+// bounded-wait self-test (k_comb.cu): a wait that nothing completes gives up
+// after `polls` polls and sets the multiply-accumulate error flag
+int wait_selftest(unsigned polls, int* gaveUp, double* seconds);
 } // namespace p2c

@@ -24,7 +24,10 @@
 //
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress and caches it; make that
-// first call before any stream capture on the device.  The call performs no
+// first call before any stream capture on the device.  The cached address is
+// valid for the life of the device's primary context: a caller that resets
+// the device (cudaDeviceReset) must not use this entry point afterwards, as
+// the module reloads and the array can move.  The call performs no
 // allocation of any kind.
 #include "common.cuh"
 #include "kernels.h"

@@ -234,7 +234,9 @@ class ResidentJob:
     def download(self, rec_host: torch.Tensor | None = None, stream=None):
         """D2H of recovery slices, IFSC entries, file MD5s and checksum verdicts
         (asynchronous on `stream`).  IFSC, MD5s and verdicts land in pinned
-        buffers owned by the job and reused by the next call."""
+        buffers owned by the job and reused by the next call: synchronise
+        `stream` before reading them, and copy them (e.g. .clone()) before
+        calling download() again if they are to be kept."""
         st = stream or torch.cuda.current_stream(self.dev)
         if not hasattr(self, "_h_small"):
             # pinned host buffers made once: allocating pinned memory per call

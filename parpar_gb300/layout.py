@@ -21,3 +21,20 @@ def file_layout(file_lens, S):
             lens.append(int(min(S, ln - k * S)) if ln else 0)
         r += n
     return np.array(first, dtype=np.uint32), np.array(lens, dtype=np.uint32)
+
+
+def file_lengths(N, files, S, seed):
+    """Seeded uneven file lengths with sum(ceil(len/S)) == N, the last slice
+    of each file partial: the file sets of the benchmark workloads."""
+    rng = np.random.default_rng(seed)
+    if files == 1:
+        return [N * S]
+    w = rng.uniform(0.5, 1.5, size=files)
+    counts = np.maximum(1, np.floor(w / w.sum() * N)).astype(int)
+    while counts.sum() < N:
+        counts[rng.integers(files)] += 1
+    while counts.sum() > N:
+        k = int(np.argmax(counts))
+        counts[k] -= 1
+    tails = rng.integers(1, S + 1, size=files)
+    return [int((c - 1) * S + t) for c, t in zip(counts, tails)]

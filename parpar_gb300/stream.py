@@ -14,9 +14,9 @@ shape (slice size, file lengths, recovery exponents):
     contraction fills the GPU on its own), its IFSC hashes (one thread per
     slice) on a side stream, so that they overlap the next contraction;
   * the file MD5 chains of each group of `group` consecutive jobs run as one
-    launch of `group x files` threads in a single block
-    (par2cuda_file_md5_pooled), on a high-priority stream of the group: one
-    SM holds all of them while later jobs' contractions use the others.
+    launch of `group x files` threads, `md5_block` of them per block
+    (par2cuda_file_md5_pooled), on a high-priority stream of the group: a
+    few SMs hold all of them while later jobs' contractions use the others.
 
 With host buffers (run(..., host_in=..., host_out=...)) every job's inputs are
 copied to its slot on a copy stream and its results (recovery slices, IFSC
@@ -39,7 +39,7 @@ from .layout import file_layout
 
 class JobStream:
     def __init__(self, slice_size: int, file_lens, exps, slots: int = 24, group: int = 8, device: int = 0,
-                 method: int = _lib.METHOD_COMB):
+                 method: int = _lib.METHOD_COMB, md5_block: int = 128):
         if slots % group:
             raise ValueError("slots must be a multiple of group")
         L = self.L = _lib.load()
@@ -51,6 +51,11 @@ class JobStream:
         self.exps = list(exps)
         self.R = R = len(self.exps)
         self.slots, self.group = slots, group
+        # file MD5 chains per block: a chain issues about one instruction per
+        # two cycles of its ~4-cycle dependency steps, so 4 warps (one per
+        # scheduler) run at full speed on one SM while more start to slow
+        # each other
+        self.md5_block = md5_block
         if group * F > 512:
             raise ValueError("group x files must be at most 512 (one block of file MD5 chains)")
         self.method = method
@@ -161,8 +166,12 @@ class JobStream:
         a = comp.cuda_stream
         _lib.check(L.par2cuda_rows_checksum(d_in, self.pw, N, self.d_lens.data_ptr(), self.S, 0, None,
                                            self.d_ck.data_ptr(), a), "rows_checksum")
+        if timing:
+            rec["mul0"] = self._event(comp, True)
         _lib.check(L.par2cuda_muladd(d_in, self.pw, N, self.d_coeff.data_ptr(), d_rec, self.pw, R, self.row_words, 0,
                                     self.method, self.d_scratch.data_ptr(), self.scratch_bytes, a), "muladd")
+        if timing:
+            rec["mul1"] = self._event(comp, True)
         _lib.check(L.par2cuda_rows_checksum(d_rec, self.pw, R, None, self.S, 1, self.d_flags[s].data_ptr(),
                                            self.d_ck.data_ptr(), a), "verify")
         self.ev_gf[s] = self._event(comp, timing)
@@ -170,7 +179,7 @@ class JobStream:
         _lib.check(L.par2cuda_slice_hash(d_in, self.pitch, N, self.d_lens.data_ptr(), self.S,
                                         self.d_ifsc[s].data_ptr(), side.cuda_stream), "slice_hash")
         self.ev_ifsc[s] = self._event(side, timing)
-        self.launches += 5   # checksum, coefficient index, contraction, verification, IFSC
+        self.launches += 7   # checksum (2 kernels), coefficient index, contraction, verification (2), IFSC
         rec["gf"], rec["ifsc"] = self.ev_gf[s], self.ev_ifsc[s]
         self.jobs_done.append(rec)
 
@@ -191,7 +200,7 @@ class JobStream:
         _lib.check(self.L.par2cuda_file_md5_pooled(self.d_in[s0 * self.N].data_ptr(), self.pitch, nf,
                                                   self.d_gflen.data_ptr() + 8 * j0 * self.F,
                                                   self.d_gfirst.data_ptr(), self.S, self.d_fmd5[s0].data_ptr(),
-                                                  512, st.cuda_stream), "file_md5_pooled")
+                                                  self.md5_block, st.cuda_stream), "file_md5_pooled")
         ev = self._event(st, timing)
         self.ev_md5[g] = ev
         self.launches += 1
@@ -227,6 +236,11 @@ class JobStream:
             t_beg = min(0.0, start.elapsed_time(rec["md5_start"]))
             out.append((t_end - t_beg) / 1e3)
         return out
+
+    def muladd_ms(self):
+        """Mean device time of the timed jobs' multiply-accumulate launches (ms)."""
+        t = [r["mul0"].elapsed_time(r["mul1"]) for r in self.jobs_done if "mul0" in r]
+        return float(np.mean(t)) if t else 0.0
 
     def clear_records(self):
         self.jobs_done = []

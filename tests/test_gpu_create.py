@@ -1,15 +1,10 @@
-"""Files on disk -> finished .par2 files through the GPU backend, checked
-packet by packet: every packet MD5, the set ID, file IDs and descriptions,
-IFSC entries against the oracle's hashes, recovery slices against the oracle
-with the inputs numbered in file-ID order, and ParPar's default file layout."""
-import hashlib
-import struct
-
+"""Files on disk -> finished .par2 files through the GPU backend, compared byte
+for byte with the files the oracle's restatement of the reference's writers
+builds from the same input bytes (oracle/par2_packets.py: lib/par2.js packet
+formats, lib/par2gen.js layout and names, IFSC / file MD5 / recovery data from
+the oracle), and parsed with par-compare's packet checks."""
 import numpy as np
 import pytest
-
-from oracle import oracle as O
-from parpar_gb300 import par2packets as P
 
 pytestmark = pytest.mark.gpu
 
@@ -37,75 +32,21 @@ def _files(tmp_path, sizes, names, seed):
 ])
 def test_create_par2_files(tmp_path, S, R, sizes, names):
     pytest.importorskip("torch")
-    from parpar_gb300.create import create, plan_files
+    from parpar_gb300.create import create
+    from oracle import par2_packets as OP
     paths = _files(tmp_path / "in", sizes, names, seed=S + R)
-    out = create(paths, S, R, str(tmp_path / "set"))
+    creator = "par2cuda test creator"
+    base = str(tmp_path / "set")
+    out = create(paths, S, R, base, creator=creator)
     data = [open(p, "rb").read() for p in paths]
-
-    # per-file facts from the bytes themselves and the oracle
-    m16 = [hashlib.md5(d[:16384]).digest() for d in data]
-    ids = [P.file_id(m16[i], sizes[i], names[i]) for i in range(len(paths))]
-    order = sorted(range(len(paths)), key=lambda i: int.from_bytes(ids[i], "little"))
-    main_body = struct.pack("<QI", S, len(ids)) + b"".join(ids[i] for i in order)
-    set_id = hashlib.md5(main_body).digest()
-
-    # recovery reference: input slices numbered in file-ID order, zero-padded
-    rows, lens = [], []
-    for i in order:
-        for k in range((sizes[i] + S - 1) // S):
-            chunk = data[i][k * S:(k + 1) * S]
-            rows.append(np.frombuffer(chunk + bytes(S - len(chunk)), dtype=np.uint8))
-            lens.append(len(chunk))
-    x = np.stack(rows)
-    rec = O.recover(x, np.array(lens), np.arange(len(rows)), list(range(R)), threads=8) if R else None
-
-    n_crit = sum(1 + (1 if sizes[i] else 0) for i in range(len(paths))) + 1
-    plan = plan_files(str(tmp_path / "set"), n_crit, R)
-    assert out == [f.name for f in plan]
-    seen_rec = set()
-    for of in plan:
-        buf = open(of.name, "rb").read()
-        pkts = list(P.parse(buf))          # validates every packet MD5 and length
-        assert all(sid == set_id for _, sid, _ in pkts)
-        kinds = []
-        for ptype, _, body in pkts:
-            if ptype == P.T_RECV:
-                e = struct.unpack_from("<I", body)[0]
-                assert body[4:] == rec[e].tobytes()
-                seen_rec.add(e)
-                kinds.append("R")
-            elif ptype == P.T_DESC:
-                fid = body[:16]
-                i = ids.index(fid)
-                assert body[16:32] == hashlib.md5(data[i]).digest()
-                assert body[32:48] == m16[i]
-                assert struct.unpack_from("<Q", body, 48)[0] == sizes[i]
-                assert body[56:].rstrip(b"\0") == names[i].encode("utf-8")
-                kinds.append("d")
-            elif ptype == P.T_UNI:
-                i = ids.index(body[:16])
-                assert body[16:].decode("utf-16-le").rstrip("\0") == names[i]
-            elif ptype == P.T_IFSC:
-                i = ids.index(body[:16])
-                ifsc, _ = O.hash_file(np.frombuffer(data[i], dtype=np.uint8), S)
-                assert body[16:] == ifsc
-                kinds.append("i")
-            elif ptype == P.T_MAIN:
-                assert body == main_body
-                kinds.append("m")
-            elif ptype == P.T_CREATOR:
-                kinds.append("C")
-            else:
-                raise AssertionError(ptype)
-        # the layout: critical packets in file-ID order (desc, ifsc), main last
-        crit_seq = []
-        for i in order:
-            crit_seq.append("d")
-            if sizes[i]:
-                crit_seq.append("i")
-        crit_seq.append("m")
-        want = []
-        for kind, k in of.packets:
-            want.append("R" if kind == "recovery" else ("C" if kind == "creator" else crit_seq[k]))
-        assert kinds == want
-    assert seen_rec == set(range(R))
+    # the oracle's restatement of lib/par2.js + lib/par2gen.js, built from the
+    # files' bytes alone: every output file byte for byte
+    names_ = OP.display_names(paths)
+    assert names_ == names
+    want, set_id = OP.expected_files(data, names_, S, R, creator)
+    assert sorted(out) == sorted(base + sfx for sfx in want)
+    for sfx, wbytes in want.items():
+        got = open(base + sfx, "rb").read()
+        pkts = OP.parse(got)               # par-compare's checks: signature, length, set ID, packet MD5
+        assert pkts and len(got) == len(wbytes)
+        assert got == wbytes, sfx

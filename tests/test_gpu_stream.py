@@ -1,0 +1,99 @@
+"""The job stream (parpar_gb300.stream.JobStream): many create jobs in flight,
+file MD5 chains of several jobs pooled in one launch.  Every job's recovery
+slices, IFSC entries, file MD5s and verdicts must equal the oracle's for that
+job's inputs, with resident inputs and with inputs copied from (and results
+copied to) pinned host buffers, including partial groups and slot reuse."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from parpar_gb300 import synth
+from parpar_gb300.layout import file_layout
+
+pytestmark = pytest.mark.gpu
+
+S = 65536
+FILE_LENS = [5 * S + 123, 3 * S, 1, 7 * S + 65535, 2 * S + 2, 40000]
+EXPS = [0, 1, 2, 300, 65534]
+
+
+def expected(x):
+    """Oracle results for one job's rows x (uint8 [N, S], tails beyond each row's length ignored)."""
+    first, lens = file_layout(FILE_LENS, S)
+    xz = x.copy()
+    for i, ln in enumerate(lens):
+        xz[i, ln:] = 0
+    rec = O.recover(xz, lens, np.arange(len(lens)), EXPS)
+    ifsc, fmd5 = b"", b""
+    for f, ln in enumerate(FILE_LENS):
+        a = int(first[f])
+        n = max(1, (ln + S - 1) // S)
+        i_, m_ = O.hash_file(x[a:a + n].reshape(-1)[:ln], S)
+        ifsc += i_
+        fmd5 += m_
+    return rec, ifsc, fmd5
+
+
+def make_stream(slots=4, group=2):
+    from parpar_gb300.stream import JobStream
+    return JobStream(S, FILE_LENS, EXPS, slots=slots, group=group)
+
+
+def test_stream_resident_jobs_match_oracle():
+    js = make_stream()
+    js.fill_synthetic(seed0=50)
+    js.run(7, first_job=0, timing=True)       # 3 full groups + a partial one, slots reused
+    js.run(3, first_job=7)                    # continues mid-group
+    torch.cuda.synchronize()
+    for s in range(js.slots):
+        x = synth.slices(50 + s, 0, js.N, S)
+        rec, ifsc, fmd5 = expected(x)
+        got_rec, got_ifsc, got_fmd5, flags = js.slot_results(s)
+        assert flags.all()
+        assert np.array_equal(got_rec, rec)
+        assert got_ifsc.tobytes() == ifsc
+        assert got_fmd5.tobytes() == fmd5
+    lat = js.latencies()
+    assert len(lat) == 7 and min(lat) > 0
+
+
+def test_stream_host_buffers_match_oracle():
+    js = make_stream(slots=4, group=2)
+    hosts = [torch.from_numpy(synth.slices(70 + k, 0, js.N, S)).pin_memory() for k in range(3)]
+    outs = js.host_out_buffers(5)
+    js.run(9, first_job=0, host_in=hosts, host_out=outs)
+    torch.cuda.synchronize()
+    want = [expected(h.numpy()) for h in hosts]
+    # job k read hosts[k % 3] and wrote outs[k % 5]; the last 5 jobs (4..8) hold the outputs
+    for k in range(4, 9):
+        rec, ifsc, fmd5 = want[k % 3]
+        o = outs[k % 5]
+        assert o[3].numpy().all()
+        assert np.array_equal(o[0].numpy(), rec)
+        assert o[1].numpy().tobytes() == ifsc
+        assert o[2].numpy().tobytes() == fmd5
+
+
+def test_pooled_file_md5_matches_per_file_launch():
+    """par2cuda_file_md5_pooled (several block sizes) = par2cuda_file_md5."""
+    from parpar_gb300 import _lib
+    L = _lib.load()
+    first, lens = file_layout(FILE_LENS * 7, S)
+    N = len(lens)
+    pitch = L.par2cuda_row_pitch_bytes(S)
+    d = torch.empty((N, pitch), dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    _lib.check(L.par2cuda_synth_fill(d.data_ptr(), pitch, N, S, 9, 0, st), "synth")
+    flen = torch.tensor(FILE_LENS * 7, dtype=torch.int64, device="cuda")
+    fr = torch.from_numpy(first.view(np.int32)).cuda()
+    nf = len(FILE_LENS) * 7
+    ref = torch.empty(nf * 16, dtype=torch.uint8, device="cuda")
+    _lib.check(L.par2cuda_file_md5(d.data_ptr(), pitch, nf, flen.data_ptr(), fr.data_ptr(), S, ref.data_ptr(), st), "md5")
+    for per in (1, 32, 64, 512):
+        out = torch.zeros(nf * 16, dtype=torch.uint8, device="cuda")
+        _lib.check(L.par2cuda_file_md5_pooled(d.data_ptr(), pitch, nf, flen.data_ptr(), fr.data_ptr(), S,
+                                             out.data_ptr(), per, st), "pooled")
+        assert torch.equal(out, ref), per
+    assert L.par2cuda_file_md5_pooled(d.data_ptr(), pitch, nf, flen.data_ptr(), fr.data_ptr(), S,
+                                      ref.data_ptr(), 48, st) < 0
