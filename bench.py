@@ -72,6 +72,13 @@ WORKLOADS = {
     "create": dict(S=2 * 1048576, N=2000, files=40, R=200, hashes=True,
                    desc="the bandwidth workload's 40 files (3.9 GiB) written to the host's disk, then PAR2 create "
                         "end to end: read, GPU hashing + recovery, .par2 index + pow2 volumes written"),
+    # ncu capture cases of the remaining kernels (no bench line): the
+    # recovery-packet MD5 over 256 x 1 MiB rows, and the persistent batched
+    # multiply-accumulate over a small mix
+    "profile_rows_md5": dict(S=1048576, N=8, files=1, R=256, hashes=False,
+                             desc="recovery-packet MD5 of 256 recovery rows x 1 MiB (ncu capture size)"),
+    "profile_batched": dict(S=0, N=0, files=0, R=0, hashes=False, jobs=12,
+                            desc="12 jobs, N 64..600, S 256 KiB..2 MiB: pass 0 persistent + grid (ncu capture size)"),
     # serving: Poisson requests, admitted by free HBM, continuous batching
     "serving": dict(S=0, N=0, files=0, R=0, hashes=False, jobs=48,
                     desc="Poisson requests (sizes as the 64-job mix) at 200/s and at a sub-saturation rate; admission by "
@@ -316,6 +323,64 @@ def run_reference(args, cfg, file_lens):
                                                                " + IFSC + file MD5 per file" if job.hashes else "")),
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": wall,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_reference_mix(args, cfg):
+    """--impl reference for the batched and serving workloads: the jobs of the
+    same seeded mix through the reference's own CPU core one after another
+    (the reference has no batching; PAR2ProcCPU with GF16_AUTO on all host
+    cores, no hashing, as the GPU mix has none).  The whole mix would take the
+    CPU minutes, so the sample is the mix's jobs in order whose estimated time
+    fits a budget of --cpu-budget seconds; jobs/s for the whole mix follows
+    from the sample's mul-adds/s, and p50/p99 are the sampled service times."""
+    from oracle import oracle as O
+    from parpar_gb300.layout import make_job_mix
+    have, why = reference_core()
+    if not have:
+        print(json.dumps({"impl": "reference", "unavailable": why}))
+        return 0
+    threads = os.cpu_count() or 1
+    jobs = make_job_mix(cfg["jobs"], seed=4 if args.workload == "batched" else 5)
+    est_rate = 90e9   # first guess of the CPU's mul-adds/s, refined by the sample
+    spent, done = 0.0, []
+    for spec in jobs:
+        if spent + spec.mul_adds / est_rate > args.cpu_budget or (spec.N + spec.R) * spec.S > 48 << 30:
+            continue
+        x = O.synth_rows(spec.seed, 0, spec.N, spec.S)
+        t0 = time.perf_counter()
+        out, valid, _, _, t = O.ref_job(x, np.full(spec.N, spec.S), np.arange(spec.N), spec.exps, threads=threads)
+        wall = time.perf_counter() - t0
+        if not valid.all():
+            raise RuntimeError("reference checksum verdict false")
+        done.append((spec, t[0]))
+        spent += wall
+        est_rate = sum(s.mul_adds for s, _ in done) / sum(w for _, w in done)
+        del x, out
+    if not done:
+        print(json.dumps({"impl": "reference", "unavailable": "no job of the mix fits the CPU budget"}))
+        return 0
+    rate = sum(s.mul_adds for s, _ in done) / sum(w for _, w in done)
+    mix = sum(s.mul_adds for s in jobs)
+    walls = [w for _, w in done]
+    info = ctypes.create_string_buffer(512)
+    O.ref().ref_host_info(info, 512)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": 1,
+        "warmup": 0, "ms_per_step": mix / rate * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u16 GF(2^16)", "data": "synthetic (seeded per-job slices)",
+        "config": {"workload": args.workload, "desc": cfg["desc"], "jobs": len(jobs)},
+        "jobs_per_s": len(jobs) / (mix / rate),
+        "p50_latency_s": float(np.percentile(walls, 50)), "p99_latency_s": float(np.percentile(walls, 99)),
+        "latency_def": "service time of each sampled job (jobs run back to back on all cores)",
+        "cpu_baseline": {"kind": "reference", "cores": threads, "value": rate, "unit": UNIT,
+                         "method": "ParPar PAR2ProcCPU, GF16_AUTO (%s), jobs back to back" % info.value.decode(),
+                         "sample": "%d of the %d jobs of the mix (in mix order, those whose estimated time fits %.0f s), "
+                                   "%.3g of %.3g mul-adds" % (len(done), len(jobs), args.cpu_budget,
+                                                               sum(s.mul_adds for s, _ in done), mix)},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
@@ -881,6 +946,35 @@ def run_create_workload(args, cfg):
     return 0
 
 
+def run_profile_case(args, cfg):
+    """The profile_* capture cases that are not multiply-accumulate workloads:
+    runs the kernel(s) once after a warm-up and prints a short JSON line."""
+    import torch
+    from parpar_gb300 import _lib
+    torch.cuda.set_device(0)
+    if args.workload == "profile_rows_md5":
+        from parpar_gb300.job import ResidentJob
+        S, N, R = cfg["S"], cfg["N"], cfg["R"]
+        job = ResidentJob(S, [N * S], list(range(R)))
+        job.fill_synthetic(seed=3)
+        job.run(hashes=False)
+        for _ in range(2):
+            md5s = job.recovery_packet_md5s(bytes(16))
+        ok = bool(job.d_flags.all()) and len(md5s) == R
+    else:
+        from parpar_gb300.batch import BatchRunner
+        from parpar_gb300.layout import make_job_mix
+        jobs = make_job_mix(cfg["jobs"], seed=9, n_range=(64, 600), s_range=(256 * 1024, 2 << 20))
+        runner = BatchRunner(jobs, budget_bytes=args.budget_gib << 30)
+        times = runner.tune_mode()
+        ok = True
+        md5s = times
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": args.workload, "ok": ok, "desc": cfg["desc"],
+                      "detail": md5s if isinstance(md5s, dict) else None}))
+    return 0 if ok else 1
+
+
 def run_batched_workload(args, cfg):
     """The uneven 64-job mix, batched (graph replay) vs per-job launches."""
     import torch
@@ -961,7 +1055,9 @@ def main():
     ap.add_argument("--slots", type=int, default=24,
                     help="jobs resident at once in the job stream of hashing workloads (1 = one job at a time)")
     ap.add_argument("--group", type=int, default=8, help="jobs whose file MD5 chains share one launch in the job stream")
-    ap.add_argument("--md5-block", type=int, default=128, help="file MD5 chains per block in the job stream (32..512)")
+    ap.add_argument("--md5-block", type=int, default=64, help="file MD5 chains per block in the job stream (32..512)")
+    ap.add_argument("--cpu-budget", type=float, default=40.0,
+                    help="seconds of CPU work in the reference arm's sample of the batched / serving mix")
     ap.add_argument("--no-dense", action="store_true", help="skip the dense-contraction figure of the default run")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline_gf.traffic")
@@ -971,9 +1067,10 @@ def main():
         return 0   # single-GPU workloads: under torchrun only rank 0 measures
     if args.workload in ("batched", "serving"):
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the %s workload is reported against this backend's per-job path" % args.workload}))
-            return 0
+            return run_reference_mix(args, cfg)
         return run_batched_workload(args, cfg) if args.workload == "batched" else run_serving_workload(args, cfg)
+    if args.workload in ("profile_rows_md5", "profile_batched"):
+        return run_profile_case(args, cfg)
     if args.workload == "create" and args.impl != "reference":
         return run_create_workload(args, cfg)
     file_lens = file_lengths(cfg["N"], cfg["files"], cfg["S"], seed=2000)

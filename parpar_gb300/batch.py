@@ -27,45 +27,14 @@ Two ways to run a mix:
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
 
 import numpy as np
 import torch
 
 from . import _lib, autotune
 from .job import par2_coefficients
+from .layout import JobSpec, make_job_mix  # noqa: F401  (re-exported)
 
-KIB, MIB = 1024, 1024 * 1024
-
-
-@dataclass
-class JobSpec:
-    N: int
-    S: int
-    R: int
-    seed: int
-    exps: list = field(default_factory=list)
-
-    @property
-    def mul_adds(self) -> int:
-        return self.N * self.R * (self.S // 2)
-
-    @property
-    def input_bytes(self) -> int:
-        return self.N * self.S
-
-
-def make_job_mix(n_jobs: int = 64, seed: int = 4, n_range=(10, 5000), s_range=(64 * KIB, 8 * MIB), r_frac=(0.01, 0.30)):
-    """Seeded uneven jobs: N log-uniform in n_range, S uniform over the 4-byte
-    multiples in s_range, R = round(U(r_frac) * N) (at least 1)."""
-    rng = np.random.default_rng(seed)
-    jobs = []
-    for j in range(n_jobs):
-        N = int(round(math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))))
-        S = int(rng.integers(s_range[0] // 4, s_range[1] // 4 + 1)) * 4
-        R = max(1, int(round(rng.uniform(*r_frac) * N)))
-        jobs.append(JobSpec(N, S, R, seed * 1000 + j, list(range(R))))
-    return jobs
 
 
 def plan_passes(jobs, budget_bytes: int):

@@ -68,5 +68,9 @@ void set_error(const char* fmt, ...);
 const char* get_error();
 }
 
+// On failure the message is recorded and the runtime's per-thread "last
+// error" is consumed, so that a non-sticky failure (e.g. an allocation that
+// does not fit) is not reported again by the next launch check.
 #define P2C_CUDA_TRY(expr) do { cudaError_t _e = (expr); if(_e != cudaSuccess) { \
+	(void)cudaGetLastError(); \
 	p2c::set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(_e)); return -1; } } while(0)

@@ -24,6 +24,17 @@ pytestmark = pytest.mark.gpu
 
 
 def small_recovery_ok():
+    """A recovery through the backend (its own threads) and a launch from this
+    thread both still work: a failed allocation must not leave a stale error
+    behind for the next launch check on the calling thread."""
+    import torch
+    L = _lib.load()
+    d = torch.empty(4096, dtype=torch.uint8, device="cuda")
+    if L.par2cuda_synth_fill(d.data_ptr(), 4096, 1, 4096, 1, 0, None) != 0:
+        return False
+    torch.cuda.synchronize()
+    if not np.array_equal(d.cpu().numpy(), synth.slices(1, 0, 1, 4096)[0]):
+        return False
     x = synth.slices(3, 0, 12, 3000)
     out, valid = create_recovery(x, np.full(12, 3000), np.arange(12), [0, 1, 5])
     return valid.all() and np.array_equal(out, O.recover(x, np.full(12, 3000), np.arange(12), [0, 1, 5]))
