@@ -490,7 +490,7 @@ def stream_measure(args, cfg, file_lens, local, rank, barrier, max_over_ranks):
     from parpar_gb300.stream import JobStream
     S, N, R = cfg["S"], cfg["N"], cfg["R"]
     js = JobStream(S, file_lens, list(range(R)), slots=args.slots, group=args.group, device=local,
-                   method=_lib.METHOD_NAMES[args.method], md5_block=args.md5_block)
+                   method=_lib.METHOD_NAMES[args.method], md5_block=args.md5_block, md5_staged=not args.md5_unstaged)
     js.fill_synthetic(seed0=1 + 1000 * rank)
     torch.cuda.synchronize()
     warm = max(args.warmup, args.group)
@@ -769,8 +769,10 @@ def run_ours(args, cfg, file_lens):
         "dtype": "u16 GF(2^16)", "data": "synthetic (seeded splitmix64 slices), inputs resident in HBM",
         "config": bench_config(args, cfg, file_lens, world),
         "step": ("one whole job of the workload; jobs stream through %d resident slots (file MD5 chains of %d jobs "
-                 "pooled in one launch, %d per block), the timed region holding every kernel of all %d jobs" %
-                 (args.slots, args.group, args.md5_block, args.steps)) if use_stream else "one whole job, jobs back to back",
+                 "pooled in one launch, %d per block, %s), the timed region holding every kernel of all %d jobs" %
+                 (args.slots, args.group, args.md5_block,
+                  "global loads" if args.md5_unstaged else "bytes staged in shared memory by bulk copies",
+                  args.steps)) if use_stream else "one whole job, jobs back to back",
         "src_GBps_x_recovery": N * S * R * world / (ms / 1e3) / 1e9,
         "method": args.method,
         "roofline_gf": rgf,
@@ -856,6 +858,7 @@ def run_serving_workload(args, cfg):
         "config": {"workload": "serving", "desc": cfg["desc"], "jobs": cfg["jobs"], "budget_GB": 150, "slots": 8},
         "jobs_per_s": sat["jobs_per_s"], "p50_latency_s": sat["p50_latency_s"], "p99_latency_s": sat["p99_latency_s"],
         "rates": out, "autotune": {str(k): v[0] for k, v in autotune.table().items()},
+        "autotune_methods": {str(k): v for k, v in autotune.method_table().items()},
         "gpu_launches": sat["gpu_launches"],
     }
     print(json.dumps(line))
@@ -1028,6 +1031,7 @@ def run_batched_workload(args, cfg):
         "batched_mode": runner.mode, "mode_pass0_ms": mode_ms,
         "small_jobs_mix": small_mix_run(args),
         "autotune": {str(k): v[0] for k, v in autotune.table().items()},
+        "autotune_methods": {str(k): v for k, v in autotune.method_table().items()},
         "gpu_launches": runner.launches_per_run() * args.steps,
         "clocks": summarize_clocks(clock_lines, 0),
     }
@@ -1056,6 +1060,8 @@ def main():
                     help="jobs resident at once in the job stream of hashing workloads (1 = one job at a time)")
     ap.add_argument("--group", type=int, default=8, help="jobs whose file MD5 chains share one launch in the job stream")
     ap.add_argument("--md5-block", type=int, default=64, help="file MD5 chains per block in the job stream (32..512)")
+    ap.add_argument("--md5-unstaged", action="store_true",
+                    help="file MD5 chains load from global memory (par2cuda_file_md5_pooled) instead of bulk-copy staging")
     ap.add_argument("--cpu-budget", type=float, default=40.0,
                     help="seconds of CPU work in the reference arm's sample of the batched / serving mix")
     ap.add_argument("--no-dense", action="store_true", help="skip the dense-contraction figure of the default run")

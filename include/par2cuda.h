@@ -185,9 +185,10 @@ int par2cuda_comb_shape_for(unsigned num_rec);
  * integer-ALU roofline (2 LOP3 per word multiply-accumulate).  No counterpart
  * in the reference. */
 int par2cuda_lop3_rate(double* ops_per_s, void* stream);
-/* Reads and clears the device-side error flag of the multiply-accumulate
- * kernels: 1 when a bounded wait inside a kernel gave up (its results are then
- * invalid), 0 otherwise, negative if the flag could not be read. */
+/* Reads and clears the device-side error flags of the multiply-accumulate and
+ * staged hash kernels: 1 when a bounded wait inside a kernel gave up (its
+ * results are then invalid), 0 otherwise, negative if a flag could not be
+ * read. */
 int par2cuda_device_error(void);
 /* Self-test of the kernels' bounded waits (no counterpart in the reference):
  * one warp waits, with the multiply-accumulate kernels' own wait helper and a
@@ -259,6 +260,16 @@ int par2cuda_file_md5_pooled(const void* d_rows, size_t pitch_bytes, unsigned nu
  * (src/gf.cc:1075-1219, lib/par2.js:243-335).  One GPU thread per row. */
 int par2cuda_rows_md5(const void* d_rows, size_t pitch_bytes, unsigned num_rows, size_t data_len,
                       const uint8_t* d_prefix, unsigned prefix_len, uint8_t* d_md5, void* stream);
+/* par2cuda_file_md5 with each file's bytes staged into shared memory ahead of
+ * its hash chain by bulk asynchronous copies (TMA, three 1 KiB chunks in
+ * flight per file), so the serial chain never waits on a cache miss while
+ * other work streams through L2.  files_per_block: 32 or 64.  Requires
+ * slice_bytes % 64 == 0 and 16-byte aligned rows.  A bounded wait that gives
+ * up sets the flag par2cuda_device_error() reports.  Same results.  No
+ * counterpart in the reference. */
+int par2cuda_file_md5_staged(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
+                             const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, unsigned files_per_block,
+                             void* stream);
 /* Copies num_rows rows of row_bytes bytes between host and device memory (or
  * within either) with one 2-D copy on `stream`: the H2D of input slices into
  * the backend's pitched rows, the D2H of recovery rows into packed host

@@ -93,6 +93,7 @@ SIGNATURES = [
     ("par2cuda_file_md5", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _vp]),
     ("par2cuda_file_md5_packed", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _vp]),
     ("par2cuda_file_md5_pooled", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _u, _vp]),
+    ("par2cuda_file_md5_staged", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _u, _vp]),
     ("par2cuda_copy_rows", _i, [_vp, _sz, _vp, _sz, _sz, _u, _vp]),
     ("par2cuda_wait_selftest", _i, [_u, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_double)]),
     ("par2cuda_rows_md5", _i, [_vp, _sz, _u, _sz, _vp, _u, _vp, _vp]),

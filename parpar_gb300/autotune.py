@@ -1,11 +1,18 @@
-"""Autotuner for the comb kernel's CTA shape (recovery rows per CTA).
+"""Autotuner: the multiply method and the comb kernel's CTA shape.
 
-The comb kernel's cost per word mul-add depends on how many recovery rows one
-CTA serves (the 256-row XOR table is built once per 8 inputs and shared by
-those rows, while accumulator registers bound the rows per CTA).  For each
-bucket of recovery counts the tuner times the candidate shapes on a small
-resident problem with the real kernel and keeps the fastest; results are
-cached per device for the process.
+Method: for each bucket of recovery counts the tuner times every
+multiply-accumulate method of the library (comb XOR-combination tables, the
+LOP3 bit-plane form, split-nibble tables, the tcgen05 tensor-core form) on a
+small resident problem through par2cuda_muladd, and keeps the fastest
+(best_method).
+
+Shape: the comb kernel's cost per word mul-add depends on how many recovery
+rows one CTA serves (the 256-row XOR table is built once per 8 inputs and
+shared by those rows, while accumulator registers bound the rows per CTA).
+For each bucket the tuner times the candidate shapes with the real kernel
+and keeps the fastest (best_shape).
+
+Results are cached per device for the process.
 """
 from __future__ import annotations
 
@@ -63,6 +70,58 @@ def _time_shape(shape: int, R: int, n: int = 256, slice_bytes: int = 262144, rep
         L.par2cuda_set_comb_shape(prev)
 
 
+METHODS = {"comb": _lib.METHOD_COMB, "xor": _lib.METHOD_XOR, "nibble": _lib.METHOD_NIBBLE,
+           "tensor": _lib.METHOD_TENSOR}
+
+
+def _time_method(method: int, R: int, n: int = 256, slice_bytes: int = 262144, reps: int = 3) -> float:
+    L = _lib.load()
+    pitch = L.par2cuda_row_pitch_bytes(slice_bytes)
+    pw = pitch // 2
+    d_in = torch.empty((n, pw), dtype=torch.int16, device="cuda")
+    _lib.check(L.par2cuda_synth_fill(d_in.data_ptr(), pitch, n, slice_bytes, 98, 0, None), "synth")
+    coeff = torch.from_numpy(np.random.default_rng(R + 1).integers(0, 65536, size=(R, n), dtype=np.uint16).view(np.int16)).cuda()
+    d_rec = torch.empty((R, pw), dtype=torch.int16, device="cuda")
+    sb = L.par2cuda_muladd_scratch_bytes(R, n)
+    scratch = torch.empty(max(sb, 256), dtype=torch.uint8, device="cuda")
+    nw = ((slice_bytes + 7) // 8 * 8 + 8) // 2
+
+    def once():
+        _lib.check(L.par2cuda_muladd(d_in.data_ptr(), pw, n, coeff.data_ptr(), d_rec.data_ptr(), pw, R, nw, 0,
+                                     method, scratch.data_ptr(), sb, None), "muladd")
+    once()
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        once()
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return best
+
+
+def best_method(R: int) -> str:
+    """Fastest multiply-accumulate method ("comb", "xor", "nibble" or
+    "tensor") for R recovery rows on this device."""
+    dev = torch.cuda.current_device()
+    key = (dev, "method", _bucket(R))
+    if key not in _cache:
+        Rb = min(_bucket(R), 384)
+        times = {name: _time_method(m, Rb) for name, m in METHODS.items()}
+        _cache[key] = min(times, key=times.get)
+        _cache[(dev, "method_times", key[2])] = times
+    return _cache[key]
+
+
+def method_table() -> dict:
+    """{recovery bucket: (best method, {method: ms})} measured so far."""
+    return {k[2]: (v, _cache.get((k[0], "method_times", k[2]))) for k, v in _cache.items()
+            if len(k) == 3 and k[1] == "method"}
+
+
 def best_shape(R: int) -> int:
     """Fastest batched comb shape (1..7) for R recovery rows on this device."""
     dev = torch.cuda.current_device()
@@ -75,10 +134,12 @@ def best_shape(R: int) -> int:
     return _cache[key]
 
 
-def warm():
+def warm(methods: bool = True):
     """Measures every bucket up front (a serving loop must not stop to tune)."""
     for b in BUCKETS:
         best_shape(min(b, 384))
+        if methods:
+            best_method(min(b, 384))
 
 
 def table() -> dict:

@@ -76,7 +76,8 @@ class _JobBufs:
 class BatchRunner:
     MODES = ("persistent", "grid")
 
-    def __init__(self, jobs, budget_bytes: int = 64 << 30, device: int = 0, shape_of=None, mode: str = "persistent"):
+    def __init__(self, jobs, budget_bytes: int = 64 << 30, device: int = 0, shape_of=None, mode: str = "persistent",
+                 method_of=None):
         if mode not in self.MODES:
             raise ValueError("mode must be one of %s" % (self.MODES,))
         self.mode = mode
@@ -87,6 +88,9 @@ class BatchRunner:
         self.P, wins = plan_passes(self.jobs, budget_bytes)
         self.bufs = [_JobBufs(self.L, j, w, self.dev) for j, w in zip(self.jobs, wins)]
         self.shape_of = shape_of or (lambda R: autotune.best_shape(R))
+        # multiply method of each job's grid launch (the persistent launch is
+        # the comb kernel's)
+        self.method_of = method_of or (lambda R: autotune.best_method(R))
         self.shapes = [self.shape_of(j.R) for j in self.jobs]
         st = torch.cuda.current_stream(self.dev).cuda_stream
         for b in self.bufs:  # coefficients -> index bytes, once per job (same for every pass)
@@ -127,10 +131,24 @@ class BatchRunner:
                                           b.d_idx.numel(), st), "muladd")
 
     def _muladd_index(self, b: _JobBufs, p: int, st):
-        """One job's window as a grid launch from its resident index bytes."""
+        """One job's window as a grid launch: the comb kernel from its resident
+        index bytes, or, where the autotuner found another method faster for
+        its recovery count, that method from the coefficients."""
         off, n = b.window(p)
-        _lib.check(self.L.par2cuda_muladd_index(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_idx.data_ptr(), b.d_rec.data_ptr(),
-                                                b.pw, b.spec.R, self._n_words(n), 0, st), "muladd_index")
+        method = self.method_of(b.spec.R)
+        if method == "comb":
+            _lib.check(self.L.par2cuda_muladd_index(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_idx.data_ptr(),
+                                                    b.d_rec.data_ptr(), b.pw, b.spec.R, self._n_words(n), 0, st),
+                       "muladd_index")
+        else:
+            # scratch of its own (made on the first, eager, call; the resident
+            # index bytes stay untouched for the persistent launch)
+            if getattr(b, "d_mscratch", None) is None:
+                b.d_mscratch = torch.empty(max(self.L.par2cuda_muladd_scratch_bytes(b.spec.R, b.spec.N), 256),
+                                           dtype=torch.uint8, device=self.dev)
+            _lib.check(self.L.par2cuda_muladd(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_coeff.data_ptr(), b.d_rec.data_ptr(),
+                                              b.pw, b.spec.R, self._n_words(n), 0, autotune.METHODS[method],
+                                              b.d_mscratch.data_ptr(), b.d_mscratch.numel(), st), "muladd")
 
     # ------------------------------------------------------------ per-job path
     def run_per_job(self, verify_cb=None):

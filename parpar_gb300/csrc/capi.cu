@@ -148,9 +148,9 @@ int par2cuda_wait_selftest(unsigned polls, int* gave_up, double* seconds) {
 }
 
 int par2cuda_device_error(void) {
-	int a = p2c::comb_error_take(), b = p2c::tc_error_take();
-	if(a < 0 || b < 0) return -1;
-	return (a || b) ? 1 : 0;
+	int a = p2c::comb_error_take(), b = p2c::tc_error_take(), c = p2c::hash_error_take();
+	if(a < 0 || b < 0 || c < 0) return -1;
+	return (a || b || c) ? 1 : 0;
 }
 
 size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in) {
@@ -164,7 +164,7 @@ int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in
 	cudaStream_t st = (cudaStream_t)stream;
 	if((in_pitch_words & 1) || (rec_pitch_words & 1)) { p2c::set_error("row pitches must be even (whole u32 pairs)"); return -1; }
 	if(method == PAR2CUDA_METHOD_XOR)
-		return p2c::xor_muladd(d_in, in_pitch_words, num_in, d_coeff, d_rec, rec_pitch_words, num_rec, n_words, accumulate, st);
+		return p2c::xor_planes_muladd(d_in, in_pitch_words, num_in, d_coeff, d_rec, rec_pitch_words, num_rec, n_words, accumulate, st);
 	if(method == PAR2CUDA_METHOD_TENSOR)
 		return p2c::tc_muladd(d_in, in_pitch_words, num_in, d_coeff, d_rec, rec_pitch_words, num_rec, n_words, accumulate, true,
 		                      d_scratch, scratch_bytes, st);
@@ -228,6 +228,12 @@ int par2cuda_synth_fill_at(void* d_dst, size_t pitch_bytes, unsigned num_rows, s
 	return p2c::synth_fill(d_dst, pitch_bytes, num_rows, row_bytes, seed, first_index, (cudaStream_t)stream, byte_offset);
 }
 
+int par2cuda_file_md5_staged(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
+                             const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, unsigned files_per_block,
+                             void* stream) {
+	return p2c::file_md5_staged(d_rows, pitch_bytes, num_files, d_file_len, d_first_row, slice_bytes, d_md5,
+	                            files_per_block, (cudaStream_t)stream);
+}
 int par2cuda_copy_rows(void* dst, size_t dst_pitch, const void* src, size_t src_pitch, size_t row_bytes,
                        unsigned num_rows, void* stream) {
 	if(!num_rows || !row_bytes) return 0;

@@ -572,7 +572,7 @@ int Engine::run_kernel(unsigned areaIdx, unsigned numInputs) {
 	const size_t nWords = row_words(S);
 	const int acc = processingAdd ? 1 : 0;
 	int rc = 0;
-	if(method == 2) rc = xor_muladd(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, sCompute);
+	if(method == 2) rc = xor_planes_muladd(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, sCompute);
 	else if(method == 3) rc = nibble_muladd_t(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, gt, sCompute);
 	else if(method == 4) rc = tc_muladd(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, true, dIdx,
 	                                    tc_scratch_bytes(R, numInputs), sCompute);

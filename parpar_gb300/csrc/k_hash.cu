@@ -97,6 +97,34 @@ __device__ __forceinline__ void md5_blocks(uint32_t st[4], uint32_t& crc, const 
 	}
 }
 
+// The same for a stream whose 64-byte blocks start at a 4-byte (not 16-byte)
+// boundary of memory: 32-bit loads, same two-block register pipeline and L2
+// prefetch.
+__device__ __forceinline__ void load_block32(const uint32_t* p, size_t b, uint32_t m[16]) {
+#pragma unroll
+	for(int q = 0; q < 16; q++) m[q] = __ldg(p + b * 16 + q);
+}
+__device__ __forceinline__ void md5_blocks32(uint32_t st[4], const uint32_t* p, size_t full) {
+	uint32_t A[16], B[16];
+	if(full > 0) load_block32(p, 0, A);
+	if(full > 1) load_block32(p, 1, B);
+	for(size_t b = 0; b < full; b += 2) {
+		uint32_t m[16];
+		if(b + P2C_MD5_L2_AHEAD < full)
+			asm volatile("prefetch.global.L2 [%0];" :: "l"(p + (b + P2C_MD5_L2_AHEAD) * 16));
+#pragma unroll
+		for(int q = 0; q < 16; q++) m[q] = A[q];
+		if(b + 2 < full) load_block32(p, b + 2, A);
+		md5_block(st, m);
+		if(b + 1 < full) {
+#pragma unroll
+			for(int q = 0; q < 16; q++) m[q] = B[q];
+			if(b + 3 < full) load_block32(p, b + 3, B);
+			md5_block(st, m);
+		}
+	}
+}
+
 // CRC32 slice-by-4 tables, built per CTA in shared memory
 struct CrcTabs { uint32_t t[4][256]; };
 
@@ -358,6 +386,175 @@ int file_md5(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_
 	return 0;
 }
 
+// ---- per-file MD5 with the bytes staged through shared memory --------------
+// One thread per file, as above, but the thread does not load its bytes from
+// global memory itself: it keeps P2C_STG_NS bulk asynchronous copies
+// (cp.async.bulk, the TMA engine) of P2C_STG_CH-byte chunks of its file in
+// flight into its own ring of shared memory, each completing on an mbarrier
+// of the ring, and hashes from shared memory.  The chain then never waits on
+// an L2 miss, whatever else the GPU runs (another job's contraction streaming
+// gigabytes through L2 evicted the prefetched lines of the register-loading
+// kernel).  Needs sliceBytes % 64 == 0 (chunks never split an MD5 block) and
+// 16-byte aligned rows; every wait is bounded (on timeout the error flag is
+// set and the chain stops; its digest is then not valid).
+#define P2C_STG_CH 1024
+#define P2C_STG_NS 3
+#define P2C_STG_STRIDE (P2C_STG_CH * P2C_STG_NS + 16)
+#define P2C_STG_WAIT (1u << 24)
+__device__ unsigned g_hash_error;
+
+__device__ __forceinline__ uint32_t hs_saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool hs_wait(uint32_t bar, uint32_t parity) {
+	for(unsigned i = 0; i < P2C_STG_WAIT; i++) {
+		uint32_t ok;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+		if(ok) return true;
+	}
+	return false;
+}
+
+template<int NT>
+__global__ void __launch_bounds__(NT) k_file_md5_staged(const uint8_t* __restrict__ rows, size_t pitch, unsigned nFiles,
+                                                        const uint64_t* __restrict__ fileLen,
+                                                        const uint32_t* __restrict__ firstRow, size_t sliceBytes,
+                                                        uint8_t* __restrict__ out)
+{
+	extern __shared__ __align__(128) uint8_t smem[];
+	const unsigned t = threadIdx.x;
+	const unsigned f = blockIdx.x * NT + t;
+	uint8_t* ring = smem + (size_t)t * P2C_STG_STRIDE;
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)NT * P2C_STG_STRIDE) + t * P2C_STG_NS;
+	const uint32_t ringA = hs_saddr(ring), barA = hs_saddr(bars);
+	for(int k = 0; k < P2C_STG_NS; k++)
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barA + 8 * k) : "memory");
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	__syncthreads();
+	if(f >= nFiles) return;
+
+	const uint64_t total = fileLen[f];
+	const uint8_t* base = rows + (size_t)firstRow[f] * pitch;
+	// chunk cursor: row r of the file, byte offset `off` inside it
+	size_t issR = 0, issOff = 0;
+	uint64_t issLeft = total;          // file bytes from the issue cursor on
+	auto issue = [&](int slot) -> uint32_t {
+		const uint64_t rowBytes = issLeft + issOff < sliceBytes ? issLeft + issOff : sliceBytes;
+		const uint32_t size = (uint32_t)min((uint64_t)P2C_STG_CH, rowBytes - issOff);
+		const uint32_t csize = (size + 15u) & ~15u;
+		const uint8_t* src = base + issR * pitch + issOff;
+		const uint32_t bar = barA + 8 * slot;
+		asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+		             :: "r"(bar), "r"(csize) : "memory");
+		asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+		             :: "r"(ringA + slot * P2C_STG_CH), "l"(src), "r"(csize), "r"(bar) : "memory");
+		issLeft -= size;
+		issOff += size;
+		if(issOff == rowBytes) { issR++; issOff = 0; }
+		return size;
+	};
+	uint32_t sizes[P2C_STG_NS];
+	uint32_t phase = 0;                // bit k: parity of slot k's next completion
+	uint32_t pend = 0;                 // bit k: slot k has a copy in flight
+	int inflight = 0;
+#pragma unroll
+	for(int k = 0; k < P2C_STG_NS; k++) {
+		sizes[k] = 0;
+		if(issLeft) { sizes[k] = issue(k); inflight++; pend |= 1u << k; }
+	}
+	uint32_t st[4];
+	md5_init(st);
+	uint32_t tail[16];
+#pragma unroll
+	for(int q = 0; q < 16; q++) tail[q] = 0;
+	uint32_t tailLen = 0;
+	bool ok = true;
+	for(int slot = 0; inflight > 0; slot = slot + 1 == P2C_STG_NS ? 0 : slot + 1) {
+		if(!hs_wait(barA + 8 * slot, (phase >> slot) & 1u)) { ok = false; break; }
+		phase ^= 1u << slot;
+		pend &= ~(1u << slot);
+		inflight--;
+		uint32_t size = 0;
+#pragma unroll
+		for(int k = 0; k < P2C_STG_NS; k++) if(k == slot) size = sizes[k];
+		const uint4* p4 = reinterpret_cast<const uint4*>(ring + slot * P2C_STG_CH);
+		const uint32_t full = size / 64;
+		uint32_t A[16];
+		if(full) {
+#pragma unroll
+			for(int q = 0; q < 4; q++) { uint4 v = p4[q]; A[4 * q] = v.x; A[4 * q + 1] = v.y; A[4 * q + 2] = v.z; A[4 * q + 3] = v.w; }
+		}
+		for(uint32_t b = 0; b < full; b++) {
+			uint32_t m[16];
+#pragma unroll
+			for(int q = 0; q < 16; q++) m[q] = A[q];
+			if(b + 1 < full) {
+#pragma unroll
+				for(int q = 0; q < 4; q++) {
+					uint4 v = p4[(b + 1) * 4 + q];
+					A[4 * q] = v.x; A[4 * q + 1] = v.y; A[4 * q + 2] = v.z; A[4 * q + 3] = v.w;
+				}
+			}
+			md5_block(st, m);
+		}
+		if(size % 64) {   // only the file's last chunk: its partial block goes to the finish
+			const uint8_t* pb = ring + slot * P2C_STG_CH + full * 64;
+			for(uint32_t k = 0; k < size % 64; k++) tail[k >> 2] |= (uint32_t)pb[k] << (8 * (k & 3));
+			tailLen = size % 64;
+		}
+		if(issLeft) {
+			// order this thread's reads of the slot before the copy that reuses it
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+#pragma unroll
+			for(int k = 0; k < P2C_STG_NS; k++) if(k == slot) sizes[k] = issue(slot);
+			inflight++;
+			pend |= 1u << slot;
+		}
+	}
+	if(!ok) {
+		atomicExch(&g_hash_error, 1u);
+		// let this chain's copies still in flight land before the block exits
+		for(int k = 0; k < P2C_STG_NS; k++)
+			if(pend >> k & 1u) hs_wait(barA + 8 * k, (phase >> k) & 1u);
+		return;
+	}
+	md5_finish(st, tail, tailLen, 0, total);
+	uint8_t* o = out + (size_t)f * 16;
+#pragma unroll
+	for(int w = 0; w < 4; w++) {
+		o[4 * w] = (uint8_t)st[w]; o[4 * w + 1] = (uint8_t)(st[w] >> 8);
+		o[4 * w + 2] = (uint8_t)(st[w] >> 16); o[4 * w + 3] = (uint8_t)(st[w] >> 24);
+	}
+}
+
+int file_md5_staged(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen,
+                    const uint32_t* dFirstRow, size_t sliceBytes, uint8_t* dOut, unsigned filesPerBlock, cudaStream_t st)
+{
+	if(!nFiles) return 0;
+	if(pitchBytes % 16 || ((uintptr_t)rows & 15)) { set_error("staged file MD5: rows must be 16-byte aligned"); return -1; }
+	if(sliceBytes % 64 || !sliceBytes) { set_error("staged file MD5: slice size must be a multiple of 64 bytes"); return -1; }
+	if(filesPerBlock != 32 && filesPerBlock != 64) { set_error("staged file MD5: 32 or 64 files per block"); return -1; }
+	const size_t smem = (size_t)filesPerBlock * (P2C_STG_STRIDE + 8 * P2C_STG_NS);
+	if(filesPerBlock == 32) {
+		P2C_CUDA_TRY(cudaFuncSetAttribute(k_file_md5_staged<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		k_file_md5_staged<32><<<(nFiles + 31) / 32, 32, smem, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen,
+		                                                             dFirstRow, sliceBytes, dOut);
+	} else {
+		P2C_CUDA_TRY(cudaFuncSetAttribute(k_file_md5_staged<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		k_file_md5_staged<64><<<(nFiles + 63) / 64, 64, smem, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen,
+		                                                             dFirstRow, sliceBytes, dOut);
+	}
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
+int hash_error_take() {
+	unsigned v = 0, z = 0;
+	if(cudaMemcpyFromSymbol(&v, g_hash_error, sizeof(v)) != cudaSuccess) return -1;
+	if(v) cudaMemcpyToSymbol(g_hash_error, &z, sizeof(z));
+	return (int)v;
+}
+
 // ---- MD5 of equal-length rows (recovery packets; MD5Multi, hasher/hasher.h:33-56)
 // row i: prefix[i] (prefixLen bytes, host-assembled packet header) followed by
 // dataLen bytes of row data.  One thread per row.
@@ -383,6 +580,20 @@ __global__ void __launch_bounds__(128) k_rows_md5(const uint8_t* rows, size_t pi
 		uint32_t nocrc = 0;
 		md5_blocks<false>(st, nocrc, NoTabs{}, reinterpret_cast<const uint4*>(p), dataLen / 64);
 		pos = dataLen / 64 * 64;
+	} else if(tailLen % 4 == 0 && dataLen >= 64 - tailLen) {
+		// a prefix of whole words (the 36-byte packet header): complete its
+		// block with data words, then the data's blocks start 4-byte aligned
+		const uint32_t* d32 = reinterpret_cast<const uint32_t*>(p);
+		const unsigned need = (64 - tailLen) / 4;
+		for(unsigned q = 0; q < need; q++) tail[(tailLen >> 2) + q] = __ldg(d32 + q);
+		md5_block(st, tail);
+#pragma unroll
+		for(int q = 0; q < 16; q++) tail[q] = 0;
+		tailLen = 0;
+		pos = (size_t)need * 4;
+		const size_t full = (dataLen - pos) / 64;
+		md5_blocks32(st, d32 + need, full);
+		pos += full * 64;
 	}
 	for(; pos < dataLen; pos++) {
 		tail[tailLen >> 2] |= (uint32_t)p[pos] << (8 * (tailLen & 3));

@@ -2,13 +2,10 @@
 // (rec[r] (^)= sum_i c(r,i) in[i] over nWords words), kept for comparison and
 // for the autotuner:
 //
-//  * xor    — the LOP3 formulation of the reference's XOR bit-dependency method
-//             (gf16/gf16_xor_*.c, xor_depends/info.md): multiplication by c is
-//             split over the 16 bits of c, P[k] ^= in & -(bit k of c), i.e. one
-//             3-input LOP3 per (coefficient bit, 32-bit word pair), and the 16
-//             partial sums are folded by Horner (x^k) at the end.  No tables,
-//             no shared memory: bound by the integer pipe (~8 LOP3 per word
-//             mul-add plus mask generation).
+//  * xor    — the bit-sliced (16 bit planes) formulation of the reference's XOR
+//             bit-dependency method (gf16/gf16_xor_*.c, xor_depends/info.md):
+//             the coefficient's 16x16 GF(2) matrix applied to 16 input planes
+//             with predicated XORs; no tables, bound by the integer pipe.
 //  * nibble — split-nibble tables (the OpenCL LOOKUP idea,
 //             gf16/controller_ocl_init.cpp:112-253, with 4 x 16-entry tables per
 //             coefficient instead of 2 x 256): c*x = T0[x&15]^T1[x>>4&15]^
@@ -18,56 +15,108 @@
 
 namespace p2c {
 
-// ------------------------------------------------------------------ xor (LOP3)
-// CTA: 8 warps; warp w handles recovery row blockIdx.y*8 + w; each lane owns
-// 8 consecutive u32 (16 words) of the CTA's 512-word tile.
-__global__ void __launch_bounds__(256) k_xor_muladd(
+// ---------------------------------------------------- xor over 16 bit planes
+// The bit-sliced form of the XOR bit-dependency method: 32 words are held as
+// 16 bit planes (plane b = bit b of each of the 32 words), and multiplying by
+// c maps the 16 input planes to 16 output planes through c's 16x16 GF(2)
+// matrix (column b = c * x^b): out[j] ^= in[b] wherever bit j of c*x^b is set.
+//
+// Warp: 32 recovery rows, one per lane; every lane sees the same input planes
+// (built with 16 warp ballots per 32 words, no shared memory), so the planes
+// of an input are made once and serve 32 rows.  Each lane walks the 256 bits
+// of its own coefficient's matrix: one predicate per bit and one predicated
+// XOR per group of 32 words (PG groups per warp = 32*PG words), i.e. about
+// (1 + PG) / (32 PG) * 256 integer ops per word mul-add — the matrix is data,
+// so the network of XORs cannot be fixed at compile time as the reference's
+// per-coefficient JIT does.  At the end each lane turns its 16 output planes
+// back into words with an in-register bit transpose.
+#define P2C_PG 4
+__device__ __forceinline__ void bit_transpose16(uint32_t (&m)[16]) {
+	// m[k] holds a 16-bit row k; afterwards m[k] bit b = old m[b] bit k
+#pragma unroll
+	for(int k = 0; k < 8; k++) { uint32_t t = ((m[k] >> 8) ^ m[k + 8]) & 0x00FFu; m[k] ^= t << 8; m[k + 8] ^= t; }
+#pragma unroll
+	for(int k = 0; k < 16; k++) if((k & 4) == 0 && k < 12) { uint32_t t = ((m[k] >> 4) ^ m[k + 4]) & 0x0F0Fu; m[k] ^= t << 4; m[k + 4] ^= t; }
+#pragma unroll
+	for(int k = 0; k < 16; k++) if((k & 2) == 0 && k < 14) { uint32_t t = ((m[k] >> 2) ^ m[k + 2]) & 0x3333u; m[k] ^= t << 2; m[k + 2] ^= t; }
+#pragma unroll
+	for(int k = 0; k < 16; k += 2) { uint32_t t = ((m[k] >> 1) ^ m[k + 1]) & 0x5555u; m[k] ^= t << 1; m[k + 1] ^= t; }
+}
+
+__global__ void __launch_bounds__(128) k_xor_planes(
 	const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn, const uint16_t* __restrict__ coeff,
 	uint16_t* __restrict__ rec, size_t recPitch, unsigned R, size_t nWords, int accumulate)
 {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	const unsigned r = blockIdx.y * 8 + warp;
-	if(r >= R) return;
-	const size_t w0 = (size_t)blockIdx.x * 512 + lane * 16;
-	if(w0 >= nWords) return;
-	uint32_t P[16][8];
+	const unsigned r = blockIdx.y * 128 + warp * 32 + lane;
+	const size_t w0 = (size_t)blockIdx.x * (32 * P2C_PG);
+	if(blockIdx.y * 128 + warp * 32 >= R) return;          // whole warp past the last row
+	const bool rowOk = r < R;
+	uint32_t acc[16][P2C_PG];
 #pragma unroll
-	for(int k = 0; k < 16; k++)
+	for(int j = 0; j < 16; j++)
 #pragma unroll
-		for(int v = 0; v < 8; v++) P[k][v] = 0;
-	const uint16_t* crow = coeff + (size_t)r * nIn;
+		for(int g = 0; g < P2C_PG; g++) acc[j][g] = 0;
+	const uint16_t* crow = coeff + (size_t)(rowOk ? r : 0) * nIn;
 	for(unsigned i = 0; i < nIn; i++) {
-		const uint32_t c = __ldg(crow + i);
-		const uint4* src = reinterpret_cast<const uint4*>(in + (size_t)i * inPitch + w0);
-		const uint4 a = __ldg(src), b = __ldg(src + 1);
-		const uint32_t d[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+		// planes of the 32*PG words of input i (word 32g + lane in lane `lane`)
+		uint32_t pl[16][P2C_PG];
+		const uint16_t* src = in + (size_t)i * inPitch + w0;
 #pragma unroll
-		for(int k = 0; k < 16; k++) {
-			const uint32_t m = 0u - ((c >> k) & 1u);
+		for(int g = 0; g < P2C_PG; g++) {
+			const size_t w = w0 + 32 * g + lane;
+			const uint32_t x = w < nWords ? (uint32_t)__ldg(src + 32 * g + lane) : 0u;
 #pragma unroll
-			for(int v = 0; v < 8; v++) P[k][v] ^= d[v] & m;  // one LOP3
+			for(int b = 0; b < 16; b++) pl[b][g] = __ballot_sync(0xFFFFFFFFu, (x >> b) & 1u);
+		}
+		uint32_t col = rowOk ? (uint32_t)__ldg(crow + i) : 0u;
+#pragma unroll
+		for(int b = 0; b < 16; b++) {
+#pragma unroll
+			for(int j = 0; j < 16; j++) {
+				if((col >> j) & 1u) {
+#pragma unroll
+					for(int g = 0; g < P2C_PG; g++) acc[j][g] ^= pl[b][g];
+				}
+			}
+			// next column: c * x^(b+1)
+			col <<= 1;
+			col = (col ^ ((col >> 16) * (P2C_POLY & 0xFFFFu))) & 0xFFFFu;
 		}
 	}
-	uint32_t* dst = reinterpret_cast<uint32_t*>(rec + (size_t)r * recPitch + w0);
+	if(!rowOk) return;
+	uint16_t* dst = rec + (size_t)r * recPitch + w0;
 #pragma unroll
-	for(int v = 0; v < 8; v++) {
-		uint32_t acc = P[15][v];
+	for(int g = 0; g < P2C_PG; g++) {
 #pragma unroll
-		for(int k = 14; k >= 0; k--) acc = mul2x2(acc) ^ P[k][v];
-		if(accumulate) acc ^= dst[v];
-		dst[v] = acc;
+		for(int half = 0; half < 2; half++) {
+			uint32_t m[16];
+#pragma unroll
+			for(int j = 0; j < 16; j++) m[j] = (acc[j][g] >> (16 * half)) & 0xFFFFu;
+			bit_transpose16(m);          // m[k] = word 32g + 16*half + k
+#pragma unroll
+			for(int k = 0; k < 16; k += 2) {
+				const size_t w = w0 + 32 * g + 16 * half + k;
+				if(w >= nWords) continue;
+				uint32_t* p = reinterpret_cast<uint32_t*>(dst + 32 * g + 16 * half + k);
+				const uint32_t v = m[k] | (m[k + 1] << 16);
+				*p = accumulate ? (*p ^ v) : v;
+			}
+		}
 	}
 }
 
-int xor_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
-               size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st)
+int xor_planes_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
+                      size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st)
 {
 	if(!R || !nWords) return 0;
-	// tiles of 512 words; rows are padded to 64-word multiples, so round the
-	// tile count down to what the pitch holds and require 16-word alignment
-	size_t nw = round_up(nWords, 16);
-	dim3 grid((unsigned)((nw + 511) / 512), (R + 7) / 8);
-	k_xor_muladd<<<grid, 256, 0, st>>>(in, inPitch, nIn, coeff, rec, recPitch, R, nw, accumulate);
+	// rows are padded to 64-word multiples: tiles of 128 words stay inside
+	// the pitch once nWords is rounded to 128 where the pitch allows it
+	const size_t tile = 32 * P2C_PG;
+	size_t nw = round_up(nWords, 2);
+	if(round_up(nWords, tile) <= inPitch && round_up(nWords, tile) <= recPitch) nw = round_up(nWords, tile);
+	dim3 grid((unsigned)((nw + tile - 1) / tile), (R + 127) / 128);
+	k_xor_planes<<<grid, 128, 0, st>>>(in, inPitch, nIn, coeff, rec, recPitch, R, nw, accumulate);
 	P2C_CUDA_TRY(cudaGetLastError());
 	return 0;
 }

@@ -56,8 +56,8 @@ int lop3_rate(double* opsPerSec, cudaStream_t st);
 int md5_chain_rate(double* bytesPerSec, cudaStream_t st);
 
 // bit-sliced LOP3 kernel and split-nibble table kernel (same contract, coefficient matrix [R][nIn])
-int xor_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
-               size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st);
+int xor_planes_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
+                      size_t recPitch, unsigned R, size_t nWords, int accumulate, cudaStream_t st);
 int nibble_muladd_t(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec,
                     size_t recPitch, unsigned R, size_t nWords, int accumulate, const GfTables& gt, cudaStream_t st);
 
@@ -85,4 +85,8 @@ int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, ui
 // bounded-wait self-test (k_comb.cu): a wait that nothing completes gives up
 // after `polls` polls and sets the multiply-accumulate error flag
 int wait_selftest(unsigned polls, int* gaveUp, double* seconds);
+// file MD5 with each chain's bytes staged into shared memory by bulk copies
+int file_md5_staged(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen,
+                    const uint32_t* dFirstRow, size_t sliceBytes, uint8_t* dOut, unsigned filesPerBlock, cudaStream_t st);
+int hash_error_take();
 } // namespace p2c

@@ -39,7 +39,7 @@ from .layout import file_layout
 
 class JobStream:
     def __init__(self, slice_size: int, file_lens, exps, slots: int = 24, group: int = 8, device: int = 0,
-                 method: int = _lib.METHOD_COMB, md5_block: int = 128):
+                 method: int = _lib.METHOD_COMB, md5_block: int = 64, md5_staged: bool = True):
         if slots % group:
             raise ValueError("slots must be a multiple of group")
         L = self.L = _lib.load()
@@ -56,6 +56,10 @@ class JobStream:
         # scheduler) run at full speed on one SM while more start to slow
         # each other
         self.md5_block = md5_block
+        # staged: each chain's bytes arrive in shared memory by bulk copies
+        # (par2cuda_file_md5_staged, 32 or 64 chains per block), so chains do
+        # not stall on L2 misses while contractions stream through L2
+        self.md5_staged = md5_staged and md5_block in (32, 64) and S % 64 == 0
         if group * F > 512:
             raise ValueError("group x files must be at most 512 (one block of file MD5 chains)")
         self.method = method
@@ -197,10 +201,10 @@ class JobStream:
         nf = len(jobs) * self.F
         if timing:
             t0 = self._event(st, True)
-        _lib.check(self.L.par2cuda_file_md5_pooled(self.d_in[s0 * self.N].data_ptr(), self.pitch, nf,
-                                                  self.d_gflen.data_ptr() + 8 * j0 * self.F,
-                                                  self.d_gfirst.data_ptr(), self.S, self.d_fmd5[s0].data_ptr(),
-                                                  self.md5_block, st.cuda_stream), "file_md5_pooled")
+        md5 = self.L.par2cuda_file_md5_staged if self.md5_staged else self.L.par2cuda_file_md5_pooled
+        _lib.check(md5(self.d_in[s0 * self.N].data_ptr(), self.pitch, nf, self.d_gflen.data_ptr() + 8 * j0 * self.F,
+                       self.d_gfirst.data_ptr(), self.S, self.d_fmd5[s0].data_ptr(), self.md5_block, st.cuda_stream),
+                   "file_md5")
         ev = self._event(st, timing)
         self.ev_md5[g] = ev
         self.launches += 1

@@ -118,3 +118,29 @@ def test_batch_descriptors_edge_jobs(shape):
     for d_rec, S, expect in want:
         got = d_rec.cpu().numpy().view(np.uint8)[:, :S]
         assert np.array_equal(got, expect)
+
+
+@pytest.mark.parametrize("method", ["xor", "nibble", "tensor"])
+def test_grid_mode_with_each_method_matches_oracle(method):
+    """The batched grid path with the autotuner's choice forced to each
+    non-comb method (the choice the tuner may make for some recovery count)."""
+    torch = pytest.importorskip("torch")
+    from parpar_gb300.batch import BatchRunner
+    jobs = small_mix(seed=5, n=5)
+    runner = BatchRunner(jobs, budget_bytes=1 << 30, mode="grid", method_of=lambda R: method)
+    runner.capture()
+    runner.run_batched()
+    torch.cuda.synchronize()
+    for b in runner.bufs:
+        got = b.d_rec.cpu().numpy().view(np.uint8)[:, : b.spec.S]
+        assert np.array_equal(got, oracle_rec(b.spec)), (method, b.spec)
+        assert bool(b.d_flags.all())
+
+
+def test_autotuner_weighs_every_method():
+    pytest.importorskip("torch")
+    from parpar_gb300 import autotune
+    m = autotune.best_method(24)
+    assert m in autotune.METHODS
+    best, times = autotune.method_table()[autotune._bucket(24)]
+    assert best == m and set(times) == set(autotune.METHODS) and min(times.values()) == times[m]

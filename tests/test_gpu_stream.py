@@ -97,3 +97,39 @@ def test_pooled_file_md5_matches_per_file_launch():
         assert torch.equal(out, ref), per
     assert L.par2cuda_file_md5_pooled(d.data_ptr(), pitch, nf, flen.data_ptr(), fr.data_ptr(), S,
                                       ref.data_ptr(), 48, st) < 0
+    for per in (32, 64):
+        out = torch.zeros(nf * 16, dtype=torch.uint8, device="cuda")
+        _lib.check(L.par2cuda_file_md5_staged(d.data_ptr(), pitch, nf, flen.data_ptr(), fr.data_ptr(), S,
+                                             out.data_ptr(), per, st), "staged")
+        assert torch.equal(out, ref), per
+    assert L.par2cuda_device_error() == 0
+    # the staged form needs whole MD5 blocks per slice and 32 or 64 files per block
+    assert L.par2cuda_file_md5_staged(d.data_ptr(), pitch, nf, flen.data_ptr(), fr.data_ptr(), S - 4,
+                                      ref.data_ptr(), 64, st) < 0
+    assert L.par2cuda_file_md5_staged(d.data_ptr(), pitch, nf, flen.data_ptr(), fr.data_ptr(), S,
+                                      ref.data_ptr(), 128, st) < 0
+
+
+def test_staged_file_md5_against_oracle_odd_lengths():
+    """Files ending at every residue of the 1 KiB chunk and the 64-byte block."""
+    from parpar_gb300 import _lib
+    L = _lib.load()
+    S = 4096
+    lens = [0, 1, 15, 16, 63, 64, 65, 1023, 1024, 1025, 4095, 4096, 4097, 3 * 4096 + 1000, 20000]
+    first, _ = file_layout(lens, S)
+    N = int(first[-1]) + max(1, -(-lens[-1] // S))
+    pitch = L.par2cuda_row_pitch_bytes(S)
+    d = torch.empty((N, pitch), dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    _lib.check(L.par2cuda_synth_fill(d.data_ptr(), pitch, N, S, 21, 0, st), "synth")
+    flen = torch.tensor(lens, dtype=torch.int64, device="cuda")
+    fr = torch.from_numpy(first.view(np.int32)).cuda()
+    out = torch.zeros(len(lens) * 16, dtype=torch.uint8, device="cuda")
+    _lib.check(L.par2cuda_file_md5_staged(d.data_ptr(), pitch, len(lens), flen.data_ptr(), fr.data_ptr(), S,
+                                         out.data_ptr(), 32, st), "staged")
+    x = synth.slices(21, 0, N, S)
+    got = out.cpu().numpy().reshape(-1, 16)
+    for f, ln in enumerate(lens):
+        a = int(first[f])
+        data = x[a:a + max(1, -(-ln // S))].reshape(-1)[:ln]
+        assert got[f].tobytes() == O.md5(data), ln

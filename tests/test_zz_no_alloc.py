@@ -1,4 +1,4 @@
-"""par2cuda_muladd_noalloc against par2cuda_muladd, through the C ABI.
+"""par2cuda_muladd_noalloc against par2cuda_muladd and the oracle, through the C ABI.
 
 The no-alloc entry point serves callers that cannot hand the library a
 scratch buffer or let it allocate one (a fixed device-memory budget, or a
@@ -62,6 +62,12 @@ def test_noalloc_matches_existing_entry_point_twice_in_a_row():
         torch.cuda.synchronize()
         # bit-exact over the words the call covers
         assert torch.equal(got[:, :nw], want[:, :nw])
+        # and against the oracle over the slice bytes
+        from oracle import oracle as O
+        from parpar_gb300 import synth
+        prod = O.recover_coeffs(synth.slices(seed, 0, n, S), np.full(n, S), coeff.cpu().numpy().view(np.uint16))
+        expect = prod.view(np.int16) ^ (start[:, : S // 2].cpu().numpy() if acc else 0)
+        assert np.array_equal(got[:, : S // 2].cpu().numpy(), expect)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
