@@ -636,6 +636,7 @@ def plugin_measure(args, cfg, file_lens, local, steps):
     return {"value": mul_adds / tp, "unit": UNIT, "h2d_bytes_per_step": int(row_lens.sum()),
             "d2h_bytes_per_step": R * S, "ms_per_step": tp * 1e3, "steps": steps,
             "ms_min_max": [min(times) * 1e3, max(times) * 1e3],
+            "ms_each": [round(t * 1e3, 2) for t in times],
             "spread": (max(times) - min(times)) / tp,
             "spread_p10_p90": float(np.percentile(times, 90) - np.percentile(times, 10)) / tp,
             "batch": inf["staging_size"], "staging_areas": inf["staging_count"], "method_desc": inf["method_desc"],

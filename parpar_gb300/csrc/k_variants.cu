@@ -24,12 +24,13 @@ namespace p2c {
 // Warp: 32 recovery rows, one per lane; every lane sees the same input planes
 // (built with 16 warp ballots per 32 words, no shared memory), so the planes
 // of an input are made once and serve 32 rows.  Each lane walks the 256 bits
-// of its own coefficient's matrix: one predicate per bit and one predicated
-// XOR per group of 32 words (PG groups per warp = 32*PG words), i.e. about
-// (1 + PG) / (32 PG) * 256 integer ops per word mul-add — the matrix is data,
-// so the network of XORs cannot be fixed at compile time as the reference's
-// per-coefficient JIT does.  At the end each lane turns its 16 output planes
-// back into words with an in-register bit transpose.
+// of its own coefficient's matrix: a mask per bit (all ones where the bit is
+// set) and one three-input LOP3, acc ^= plane & mask, per group of 32 words
+// (PG groups per warp = 32*PG words), i.e. about (2 + PG) / (32 PG) * 256
+// integer ops per word mul-add — the matrix is data, so the network of XORs
+// cannot be fixed at compile time as the reference's per-coefficient JIT does.
+// At the end each lane turns its 16 output planes back into words with an
+// in-register bit transpose.
 #define P2C_PG 4
 __device__ __forceinline__ void bit_transpose16(uint32_t (&m)[16]) {
 	// m[k] holds a 16-bit row k; afterwards m[k] bit b = old m[b] bit k
@@ -67,17 +68,23 @@ __global__ void __launch_bounds__(128) k_xor_planes(
 			const size_t w = w0 + 32 * g + lane;
 			const uint32_t x = w < nWords ? (uint32_t)__ldg(src + 32 * g + lane) : 0u;
 #pragma unroll
-			for(int b = 0; b < 16; b++) pl[b][g] = __ballot_sync(0xFFFFFFFFu, (x >> b) & 1u);
+			for(int b = 0; b < 16; b++) {
+				// all 32 lanes vote here, outside any lane-dependent control flow
+				uint32_t v;
+				asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %1, 0;\n\tvote.sync.ballot.b32 %0, q, 0xffffffff;\n\t}"
+				             : "=r"(v) : "r"((x >> b) & 1u));
+				pl[b][g] = v;
+			}
 		}
 		uint32_t col = rowOk ? (uint32_t)__ldg(crow + i) : 0u;
 #pragma unroll
 		for(int b = 0; b < 16; b++) {
 #pragma unroll
 			for(int j = 0; j < 16; j++) {
-				if((col >> j) & 1u) {
+				// all-ones when bit j of c*x^b is set: out plane j takes in plane b
+				const uint32_t m = (uint32_t)((int32_t)(col << (31 - j)) >> 31);
 #pragma unroll
-					for(int g = 0; g < P2C_PG; g++) acc[j][g] ^= pl[b][g];
-				}
+				for(int g = 0; g < P2C_PG; g++) acc[j][g] ^= pl[b][g] & m;   // one LOP3
 			}
 			// next column: c * x^(b+1)
 			col <<= 1;
