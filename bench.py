@@ -639,6 +639,7 @@ def plugin_measure(args, cfg, file_lens, local, steps):
             "ms_each": [round(t * 1e3, 2) for t in times],
             "spread": (max(times) - min(times)) / tp,
             "spread_p10_p90": float(np.percentile(times, 90) - np.percentile(times, 10)) / tp,
+            "spread_iqr": float(np.percentile(times, 75) - np.percentile(times, 25)) / tp,
             "batch": inf["staging_size"], "staging_areas": inf["staging_count"], "method_desc": inf["method_desc"],
             "path": "C ABI plugin calls from the host: wait_for_add + add_input x N (pinned host slices), "
                     "end_input, get_output x R, verdicts by output_valid; GF multiply-accumulate + internal "
