@@ -759,7 +759,8 @@ def run_ours(args, cfg, file_lens):
     sm_mhz = (clocks or {}).get("sm_mhz") or (peaks or {}).get("sm_max_mhz") or 2070.0
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     kname = _lib.comb_kernel_name(L.par2cuda_comb_shape_for(R)) if args.method in ("comb", "auto") else \
-        {"xor": "k_xor_muladd", "nibble": "k_nibble_muladd", "tensor": "k_tc_muladd"}[args.method]
+        {"xor": "k_xor_planes", "nibble": "k_nibble_muladd", "tensor": "k_tc_muladd",
+         "tensor_fp4": "k_tc4_gemm"}[args.method]
     alg_bytes = (N + R) * S  # read every input once, write every recovery once
     hbm_peak = (peaks or {}).get("hbm_gbs", 6800.0)
     rgf = roofline_gf(mul_adds, muladd_ms, lop3.value, n_sm, sm_mhz, kname, alg_bytes)
@@ -1053,7 +1054,7 @@ def main():
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-plugin", action="store_true", help="skip the plugin-boundary e2e measurement")
     ap.add_argument("--plugin-steps", type=int, default=9)
-    ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor"], default="comb",
+    ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor", "tensor_fp4"], default="comb",
                     help="multiply-accumulate kernel of the resident-job workloads")
     ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")
     ap.add_argument("--comb-shape", type=int, default=0,

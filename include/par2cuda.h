@@ -55,7 +55,8 @@ enum {
 	PAR2CUDA_METHOD_COMB = 1,   /* shared-memory XOR-combination tables (default) */
 	PAR2CUDA_METHOD_XOR = 2,    /* LOP3, per-coefficient-bit masks */
 	PAR2CUDA_METHOD_NIBBLE = 3, /* shared-memory split-nibble tables */
-	PAR2CUDA_METHOD_TENSOR = 4  /* tcgen05 GF(2) bit-matrix product (e4m3 0/1, fp32 accumulators) */
+	PAR2CUDA_METHOD_TENSOR = 4, /* tcgen05 GF(2) bit-matrix product (e4m3 0/1, fp32 accumulators) */
+	PAR2CUDA_METHOD_TENSOR_FP4 = 5 /* tcgen05 block-scaled 4-bit (mxf4) GF(2) product, TMA-fed; device level only */
 };
 
 typedef struct par2cuda_info {
@@ -199,6 +200,12 @@ int par2cuda_device_error(void);
 int par2cuda_wait_selftest(unsigned polls, int* gave_up, double* seconds);
 /* Scratch bytes par2cuda_muladd needs for (num_rec, num_in). */
 size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in);
+/* Scratch bytes par2cuda_muladd needs for method PAR2CUDA_METHOD_TENSOR_FP4:
+ * the coefficient bit matrix (16 * roundup(num_rec, 16) rows of
+ * roundup(num_in, 16) * 8 bytes) plus the 4-bit input planes of a chunk of at
+ * most 1 GiB of words (more scratch = larger chunks; at least one 128-word
+ * tile).  No counterpart in the reference. */
+size_t par2cuda_tensor_fp4_scratch_bytes(unsigned num_rec, unsigned num_in, size_t n_words);
 /* rec[r][0..n_words) (^)= sum_i coeff[r*num_in + i] * in[i][0..n_words),
  * the run_kernel body (gf16/controller_cpu.cpp:488-515).  Pitches are in
  * 16-bit words (even); rows must be readable/writable up to

@@ -15,9 +15,9 @@ DONE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int)
 PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint)
 
 ADD_OK, ADD_OK_BUSY, ADD_FULL = 0, 1, 2
-METHOD_AUTO, METHOD_COMB, METHOD_XOR, METHOD_NIBBLE, METHOD_TENSOR = 0, 1, 2, 3, 4
+METHOD_AUTO, METHOD_COMB, METHOD_XOR, METHOD_NIBBLE, METHOD_TENSOR, METHOD_TENSOR_FP4 = 0, 1, 2, 3, 4, 5
 METHOD_NAMES = {"auto": METHOD_AUTO, "comb": METHOD_COMB, "xor": METHOD_XOR, "nibble": METHOD_NIBBLE,
-                "tensor": METHOD_TENSOR}
+                "tensor": METHOD_TENSOR, "tensor_fp4": METHOD_TENSOR_FP4}
 
 
 def comb_kernel_name(shape: int) -> str:
@@ -95,6 +95,7 @@ SIGNATURES = [
     ("par2cuda_file_md5_pooled", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _u, _vp]),
     ("par2cuda_file_md5_staged", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _u, _vp]),
     ("par2cuda_copy_rows", _i, [_vp, _sz, _vp, _sz, _sz, _u, _vp]),
+    ("par2cuda_tensor_fp4_scratch_bytes", _sz, [_u, _u, _sz]),
     ("par2cuda_wait_selftest", _i, [_u, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_double)]),
     ("par2cuda_rows_md5", _i, [_vp, _sz, _u, _sz, _vp, _u, _vp, _vp]),
     ("par2cuda_synth_fill", _i, [_vp, _sz, _u, _sz, _u64, _u64, _vp]),

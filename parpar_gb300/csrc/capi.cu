@@ -148,14 +148,18 @@ int par2cuda_wait_selftest(unsigned polls, int* gave_up, double* seconds) {
 }
 
 int par2cuda_device_error(void) {
-	int a = p2c::comb_error_take(), b = p2c::tc_error_take(), c = p2c::hash_error_take();
-	if(a < 0 || b < 0 || c < 0) return -1;
-	return (a || b || c) ? 1 : 0;
+	int a = p2c::comb_error_take(), b = p2c::tc_error_take(), c = p2c::hash_error_take(), d = p2c::tc4_error_take();
+	if(a < 0 || b < 0 || c < 0 || d < 0) return -1;
+	return (a || b || c || d) ? 1 : 0;
 }
 
 size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in) {
 	// enough for every method: comb index bytes, tensor bit-matrix rows
 	return p2c::round_up(std::max(p2c::idx_bytes(num_rec, num_in), p2c::tc_scratch_bytes(num_rec, num_in)), 256);
+}
+
+size_t par2cuda_tensor_fp4_scratch_bytes(unsigned num_rec, unsigned num_in, size_t n_words) {
+	return p2c::tc4_scratch_bytes(num_rec, num_in, n_words);
 }
 
 int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in, const uint16_t* d_coeff,
@@ -165,6 +169,9 @@ int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in
 	if((in_pitch_words & 1) || (rec_pitch_words & 1)) { p2c::set_error("row pitches must be even (whole u32 pairs)"); return -1; }
 	if(method == PAR2CUDA_METHOD_XOR)
 		return p2c::xor_planes_muladd(d_in, in_pitch_words, num_in, d_coeff, d_rec, rec_pitch_words, num_rec, n_words, accumulate, st);
+	if(method == PAR2CUDA_METHOD_TENSOR_FP4)
+		return p2c::tc4_muladd(d_in, in_pitch_words, num_in, d_coeff, d_rec, rec_pitch_words, num_rec, n_words, accumulate,
+		                       d_scratch, scratch_bytes, st);
 	if(method == PAR2CUDA_METHOD_TENSOR)
 		return p2c::tc_muladd(d_in, in_pitch_words, num_in, d_coeff, d_rec, rec_pitch_words, num_rec, n_words, accumulate, true,
 		                      d_scratch, scratch_bytes, st);

@@ -1,0 +1,374 @@
+// The GF(2^16) contraction as a block-scaled 4-bit matrix product on tcgen05
+// (kind::mxf4), with both operands loaded by TMA.
+//
+//   D[w][16r + j] = sum_{i,b} A[w][16i + b] * B[16r + j][16i + b]
+//   A[w][16i + b] = bit b of in_i[w]                    (input bit planes)
+//   B[16r+j][16i+b] = bit j of (c(r,i) * x^b)           (the 16x16 GF(2) matrix of c)
+//   bit j of rec_r[w] = D[w][16r + j] mod 2
+//
+// Operands are e2m1 values 0 and 1.0 (nibble 0x2), two per byte, K-major;
+// their block scale factors are all 1.0 (ue8m0 0x7F), so every product is
+// exactly 0 or 1 and the fp32 accumulators hold exact integers (< 2^24 for
+// fewer than 2^20 inputs).  Both operands are expanded once per call into
+// scratch in HBM by two preparation kernels: the inputs 4x (k_tc4_prep_in: a
+// word chunk of the inputs at a time), the coefficient matrix to its bit rows
+// (k_tc4_prep_coeff).
+//
+// GEMM CTA (128 threads): one 128-word x 256-bit-row tile (16 recovery
+// slices), all K.  Thread 0 issues the TMA loads of a 4-stage ring (A: 128
+// rows x 128 bytes, B: 256 rows x 128 bytes, 128-byte swizzle) completing on
+// "full" mbarriers; thread 32 issues 4 MMAs (M=128, N=256, K=64) per stage and
+// commits each stage to its "empty" mbarrier; the fp32 accumulators live in
+// TMEM columns 0-255, the scale factors (all 1.0) in columns 256-511.  The
+// epilogue reads the accumulators with tcgen05.ld: each thread owns one word
+// and 256 columns, i.e. 16 recovery words, whose bits are the accumulators'
+// parities.  CTAs run in groups of T4_GM word tiles that walk the recovery
+// tiles together, so a group's operand rows are read from HBM about once.
+// Every wait is bounded (error flag g_tc4_error, no hang).
+#include "common.cuh"
+#include "kernels.h"
+
+#include <cuda.h>   // CUtensorMap and its enums (types only; the encoder comes from the runtime)
+
+namespace p2c {
+
+#define T4_BM 128
+#define T4_BN 256
+#define T4_KB 128
+#define T4_NST 4
+#define T4_STAGE_A (T4_BM * T4_KB)
+#define T4_STAGE_B (T4_BN * T4_KB)
+#define T4_STAGE (T4_STAGE_A + T4_STAGE_B)
+#define T4_GM 8
+#define T4_WAIT (1u << 24)
+#define T4_A_CHUNK_BYTES (1ull << 30)
+
+__device__ unsigned g_tc4_error;
+
+// ------------------------------------------------------------------ operands
+// 4 bits -> 4 nibbles holding e2m1 1.0 (0x2) where the bit is set
+__device__ __forceinline__ uint32_t t4_spread4(uint32_t t) {
+	return ((t | (t << 3) | (t << 6) | (t << 9)) & 0x1111u) << 1;
+}
+// 16 bits -> 8 bytes, bit k in nibble k (element 2h in the low nibble of byte h)
+__device__ __forceinline__ uint2 t4_spread16(uint32_t x) {
+	return make_uint2(t4_spread4(x & 15u) | (t4_spread4((x >> 4) & 15u) << 16),
+	                  t4_spread4((x >> 8) & 15u) | (t4_spread4((x >> 12) & 15u) << 16));
+}
+
+// A chunk: rows w = w0 .. w0 + rows-1 (zero past nWords), 8 bytes per input
+// (zero for inputs >= nIn up to kBytes / 8).  Block: 64 inputs x 64 words.
+__global__ void __launch_bounds__(256) k_tc4_prep_in(const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
+                                                   size_t nWords, size_t w0, uint8_t* __restrict__ A, size_t kBytes)
+{
+	__shared__ uint16_t tile[64][65];
+	const unsigned i0 = blockIdx.y * 64;
+	const size_t wt = w0 + (size_t)blockIdx.x * 64;
+	for(int e = threadIdx.x; e < 64 * 64; e += 256) {
+		const int ii = e >> 6, ww = e & 63;
+		const unsigned i = i0 + ii;
+		const size_t w = wt + ww;
+		tile[ii][ww] = (i < nIn && w < nWords) ? __ldg(in + (size_t)i * inPitch + w) : (uint16_t)0;
+	}
+	__syncthreads();
+	const int ii = threadIdx.x & 63;
+	if((size_t)(i0 + ii) * 8 >= kBytes) return;
+	for(int ww = threadIdx.x >> 6; ww < 64; ww += 4) {
+		const uint2 v = t4_spread16(tile[ii][ww]);
+		*reinterpret_cast<uint2*>(A + ((size_t)blockIdx.x * 64 + ww) * kBytes + (size_t)(i0 + ii) * 8) = v;
+	}
+}
+
+// B: rows 16r + j for r < rPad (zero rows past R), 8 bytes per input; one
+// thread per (r, i).
+__global__ void __launch_bounds__(256) k_tc4_prep_coeff(const uint16_t* __restrict__ coeff, unsigned R, unsigned nIn,
+                                                      unsigned rPad, unsigned nInPad, uint8_t* __restrict__ B)
+{
+	const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if(id >= (size_t)rPad * nInPad) return;
+	const unsigned r = (unsigned)(id / nInPad), i = (unsigned)(id % nInPad);
+	uint32_t m[16];
+	m[0] = (r < R && i < nIn) ? __ldg(coeff + (size_t)r * nIn + i) : 0u;
+#pragma unroll
+	for(int b = 1; b < 16; b++) {
+		const uint32_t v = m[b - 1] << 1;
+		m[b] = (v ^ ((v >> 16) * (P2C_POLY & 0xFFFFu))) & 0xFFFFu;
+	}
+	// transpose: rows[j] bit b = bit j of c * x^b
+#pragma unroll
+	for(int k = 0; k < 8; k++) { uint32_t t = ((m[k] >> 8) ^ m[k + 8]) & 0x00FFu; m[k] ^= t << 8; m[k + 8] ^= t; }
+#pragma unroll
+	for(int k = 0; k < 16; k++) if((k & 4) == 0 && k < 12) { uint32_t t = ((m[k] >> 4) ^ m[k + 4]) & 0x0F0Fu; m[k] ^= t << 4; m[k + 4] ^= t; }
+#pragma unroll
+	for(int k = 0; k < 16; k++) if((k & 2) == 0 && k < 14) { uint32_t t = ((m[k] >> 2) ^ m[k + 2]) & 0x3333u; m[k] ^= t << 2; m[k + 2] ^= t; }
+#pragma unroll
+	for(int k = 0; k < 16; k += 2) { uint32_t t = ((m[k] >> 1) ^ m[k + 1]) & 0x5555u; m[k] ^= t << 1; m[k + 1] ^= t; }
+	const size_t kBytes = (size_t)nInPad * 8;
+#pragma unroll
+	for(int j = 0; j < 16; j++)
+		*reinterpret_cast<uint2*>(B + ((size_t)r * 16 + j) * kBytes + (size_t)i * 8) = t4_spread16(m[j]);
+}
+
+// ------------------------------------------------------------------ GEMM
+__device__ __forceinline__ uint32_t t4_saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool t4_wait(uint32_t bar, uint32_t parity) {
+	for(unsigned i = 0; i < T4_WAIT; i++) {
+		uint32_t ok;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+		if(ok) return true;
+	}
+	atomicExch(&g_tc4_error, 1u);
+	return false;
+}
+
+// K-major operand in shared memory, 128-byte swizzle: 8-row atoms 1024 bytes apart
+__device__ __forceinline__ uint64_t t4_desc(uint32_t saddr) {
+	uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+	d |= (uint64_t)1 << 16;
+	d |= (uint64_t)(1024 >> 4) << 32;
+	d |= (uint64_t)1 << 46;
+	d |= (uint64_t)2 << 61;
+	return d;
+}
+
+// instruction descriptor of the block-scaled kinds: A and B e2m1 (mxf4 code
+// 1), K-major, N >> 3, ue8m0 scale factors, M >> 4, scale-factor ids 0
+__device__ __forceinline__ uint32_t t4_idesc() {
+	return (1u << 7) | (1u << 10) | ((uint32_t)(T4_BN >> 3) << 17) | (1u << 23) | ((uint32_t)(T4_BM >> 4) << 24);
+}
+
+__global__ void __launch_bounds__(128, 1) k_tc4_gemm(const __grid_constant__ CUtensorMap tmA,
+                                                   const __grid_constant__ CUtensorMap tmB,
+                                                   uint16_t* __restrict__ rec, size_t recPitch, unsigned R,
+                                                   unsigned kBlocks, unsigned mTiles, unsigned nTiles,
+                                                   size_t w0, size_t nWords, int accumulate)
+{
+	extern __shared__ __align__(1024) uint8_t smem_raw[];
+	const uint32_t raw = t4_saddr(smem_raw);
+	const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
+	uint8_t* sm = smem_raw + pad;
+	const uint32_t sbase = raw + pad;
+	const uint32_t barBase = sbase + T4_NST * T4_STAGE;        // full[NST], empty[NST], done
+	uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + T4_NST * T4_STAGE + (2 * T4_NST + 1) * 8);
+	const uint32_t doneBar = barBase + 8u * (2 * T4_NST);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+	// raster: groups of T4_GM word tiles walk the recovery tiles together
+	const unsigned t = blockIdx.x;
+	const unsigned grp = t / (T4_GM * nTiles);
+	const unsigned gm = min((unsigned)T4_GM, mTiles - grp * T4_GM);
+	const unsigned within = t - grp * T4_GM * nTiles;
+	const unsigned mt = grp * T4_GM + within % gm, nt = within / gm;
+
+	if(threadIdx.x == 0) {
+		for(int s = 0; s < T4_NST; s++) {
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barBase + 8u * s) : "memory");
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barBase + 8u * (T4_NST + s)) : "memory");
+		}
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(doneBar) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		asm volatile("prefetch.tensormap [%0];" :: "l"(&tmA) : "memory");
+		asm volatile("prefetch.tensormap [%0];" :: "l"(&tmB) : "memory");
+	}
+	if(warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(t4_saddr(tslot)), "r"(512u) : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	const uint32_t tmem = *tslot;
+
+	// scale factors: TMEM columns 256-511 of every lane hold ue8m0 1.0 bytes
+	{
+		const uint32_t one = 0x7F7F7F7Fu;
+		const uint32_t lane0 = (uint32_t)(32 * warp) << 16;
+#pragma unroll
+		for(int q = 0; q < 8; q++)
+			asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+			             "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};"
+			             :: "r"(tmem + lane0 + 256 + 32 * q), "r"(one) : "memory");
+		asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+	if(threadIdx.x == 0) {
+		// TMA producer
+		for(unsigned kb = 0; kb < kBlocks; kb++) {
+			const unsigned s = kb % T4_NST;
+			if(kb >= T4_NST && !t4_wait(barBase + 8u * (T4_NST + s), ((kb / T4_NST) - 1) & 1)) break;
+			const uint32_t full = barBase + 8u * s;
+			const uint32_t dA = sbase + s * T4_STAGE, dB = dA + T4_STAGE_A;
+			asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+			             :: "r"(full), "r"((uint32_t)T4_STAGE) : "memory");
+			const int x = (int)(kb * T4_KB);
+			asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+			             :: "r"(dA), "l"(&tmA), "r"(x), "r"((int)(mt * T4_BM)), "r"(full) : "memory");
+			asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+			             :: "r"(dB), "l"(&tmB), "r"(x), "r"((int)(nt * T4_BN)), "r"(full) : "memory");
+		}
+	} else if(threadIdx.x == 32) {
+		// MMA issuer
+		const uint32_t idesc = t4_idesc();
+		const uint32_t sfa = tmem + 256, sfb = tmem + 384;
+		for(unsigned kb = 0; kb < kBlocks; kb++) {
+			const unsigned s = kb % T4_NST;
+			if(!t4_wait(barBase + 8u * s, (kb / T4_NST) & 1)) break;
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+			const uint32_t aS = sbase + s * T4_STAGE, bS = aS + T4_STAGE_A;
+#pragma unroll
+			for(int k = 0; k < 4; k++) {
+				const uint64_t ad = t4_desc(aS + k * 32), bd = t4_desc(bS + k * 32);
+				const uint32_t acc = (kb | k) != 0;
+				asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
+				             "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], [%5], p;\n\t}"
+				             :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(sfa), "r"(sfb), "r"(acc) : "memory");
+			}
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+			             :: "r"(barBase + 8u * (T4_NST + s)) : "memory");
+		}
+		asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(doneBar) : "memory");
+	}
+	__syncwarp();
+
+	// epilogue: thread (warp, lane) owns word mt*128 + 32*warp + lane and the
+	// 256 accumulator columns of its TMEM lane = 16 recovery words
+	const bool ok = t4_wait(doneBar, 0);
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	if(ok) {
+		const size_t w = w0 + (size_t)mt * T4_BM + 32 * warp + lane;
+		const uint32_t lane0 = (uint32_t)(32 * warp) << 16;
+#pragma unroll 1
+		for(int q = 0; q < 8; q++) {
+			uint32_t v[32];
+			asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+			             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+			             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+			             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+			               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+			               "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+			               "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+			             : "r"(tmem + lane0 + 32 * q));
+			asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+			uint32_t word0 = 0, word1 = 0;
+#pragma unroll
+			for(int c = 0; c < 16; c++) {
+				word0 |= (__float2uint_rz(__uint_as_float(v[c])) & 1u) << c;
+				word1 |= (__float2uint_rz(__uint_as_float(v[16 + c])) & 1u) << c;
+			}
+			const unsigned r0 = nt * 16 + 2 * q;
+			if(w < nWords) {
+				if(r0 < R) {
+					uint16_t* p = rec + (size_t)r0 * recPitch + w;
+					*p = accumulate ? (uint16_t)(*p ^ word0) : (uint16_t)word0;
+				}
+				if(r0 + 1 < R) {
+					uint16_t* p = rec + (size_t)(r0 + 1) * recPitch + w;
+					*p = accumulate ? (uint16_t)(*p ^ word1) : (uint16_t)word1;
+				}
+			}
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	if(warp == 0)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(512u) : "memory");
+}
+
+// ------------------------------------------------------------------ host
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn t4_encoder() {
+	static EncodeTiledFn fn = nullptr;
+	if(!fn) {
+		void* p = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+		   q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<EncodeTiledFn>(p);
+	}
+	return fn;
+}
+
+static int t4_map(CUtensorMap* m, const void* base, size_t rowBytes, size_t rows, unsigned boxRows) {
+	EncodeTiledFn enc = t4_encoder();
+	if(!enc) { set_error("tensor method: cuTensorMapEncodeTiled is not available"); return -1; }
+	const cuuint64_t dims[2] = {rowBytes, rows};
+	const cuuint64_t strides[1] = {rowBytes};
+	const cuuint32_t box[2] = {T4_KB, boxRows};
+	const cuuint32_t estr[2] = {1, 1};
+	CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, estr,
+	                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+	                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	if(r != CUDA_SUCCESS) { set_error("tensor method: cuTensorMapEncodeTiled failed (%d)", (int)r); return -1; }
+	return 0;
+}
+
+static size_t t4_kbytes(unsigned nIn) { return (size_t)round_up(nIn ? nIn : 1, 16) * 8; }
+static size_t t4_bbytes(unsigned R, unsigned nIn) { return (size_t)round_up(R ? R : 1, 16) * 16 * t4_kbytes(nIn); }
+
+size_t tc4_scratch_bytes(unsigned R, unsigned nIn, size_t nWords) {
+	const size_t aFull = round_up(nWords ? nWords : 1, T4_BM) * t4_kbytes(nIn);
+	const size_t aMax = std::max<size_t>(T4_A_CHUNK_BYTES, (size_t)T4_BM * t4_kbytes(nIn));
+	return round_up(t4_bbytes(R, nIn), 1024) + round_up(std::min(aFull, aMax), 1024);
+}
+
+int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec, size_t recPitch,
+               unsigned R, size_t nWords, int accumulate, void* scratch, size_t scratchBytes, cudaStream_t st)
+{
+	if(!R || !nWords) return 0;
+	if(!nIn) {
+		if(!accumulate) P2C_CUDA_TRY(cudaMemset2DAsync(rec, recPitch * 2, 0, nWords * 2, R, st));
+		return 0;
+	}
+	const size_t kBytes = t4_kbytes(nIn);
+	const unsigned nInPad = (unsigned)(kBytes / 8), rPad = (unsigned)round_up(R, 16);
+	const size_t bBytes = round_up(t4_bbytes(R, nIn), 1024);
+	if(!scratch || scratchBytes < bBytes + (size_t)T4_BM * kBytes) {
+		set_error("tensor method (mxf4) needs at least %zu bytes of scratch, %zu given", bBytes + (size_t)T4_BM * kBytes,
+		          scratchBytes);
+		return -1;
+	}
+	uint8_t* B = reinterpret_cast<uint8_t*>(scratch);
+	uint8_t* A = B + bBytes;
+	// words per chunk: what the rest of the scratch holds, in whole 128-word tiles
+	size_t wChunk = (scratchBytes - bBytes) / kBytes / T4_BM * T4_BM;
+	wChunk = std::min(wChunk, round_up(nWords, T4_BM));
+	const size_t nB = (size_t)rPad * nInPad;
+	k_tc4_prep_coeff<<<(unsigned)((nB + 255) / 256), 256, 0, st>>>(coeff, R, nIn, rPad, nInPad, B);
+	P2C_CUDA_TRY(cudaGetLastError());
+	CUtensorMap tmB;
+	if(t4_map(&tmB, B, kBytes, (size_t)rPad * 16, T4_BN)) return -1;
+	const size_t smem = T4_NST * T4_STAGE + (2 * T4_NST + 1) * 8 + 16 + 1024;
+	P2C_CUDA_TRY(cudaFuncSetAttribute(k_tc4_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const unsigned nTiles = rPad / 16;
+	const unsigned kBlocks = (unsigned)(kBytes / T4_KB);
+	for(size_t w0 = 0; w0 < nWords; w0 += wChunk) {
+		const size_t rows = std::min(wChunk, round_up(nWords - w0, T4_BM));
+		dim3 pg((unsigned)(rows / 64), (nInPad + 63) / 64);
+		k_tc4_prep_in<<<pg, 256, 0, st>>>(in, inPitch, nIn, nWords, w0, A, kBytes);
+		P2C_CUDA_TRY(cudaGetLastError());
+		CUtensorMap tmA;
+		if(t4_map(&tmA, A, kBytes, rows, T4_BM)) return -1;
+		const unsigned mTiles = (unsigned)(rows / T4_BM);
+		k_tc4_gemm<<<mTiles * nTiles, 128, smem, st>>>(tmA, tmB, rec, recPitch, R, kBlocks, mTiles, nTiles, w0, nWords,
+		                                               accumulate);
+		P2C_CUDA_TRY(cudaGetLastError());
+	}
+	return 0;
+}
+
+int tc4_error_take() {
+	unsigned v = 0, z = 0;
+	if(cudaMemcpyFromSymbol(&v, g_tc4_error, sizeof(v)) != cudaSuccess) return -1;
+	if(v) cudaMemcpyToSymbol(g_tc4_error, &z, sizeof(z));
+	return (int)v;
+}
+
+} // namespace p2c

@@ -89,4 +89,9 @@ int wait_selftest(unsigned polls, int* gaveUp, double* seconds);
 int file_md5_staged(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen,
                     const uint32_t* dFirstRow, size_t sliceBytes, uint8_t* dOut, unsigned filesPerBlock, cudaStream_t st);
 int hash_error_take();
+// block-scaled 4-bit tcgen05 form (k_tc4.cu)
+size_t tc4_scratch_bytes(unsigned R, unsigned nIn, size_t nWords);
+int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec, size_t recPitch,
+               unsigned R, size_t nWords, int accumulate, void* scratch, size_t scratchBytes, cudaStream_t st);
+int tc4_error_take();
 } // namespace p2c

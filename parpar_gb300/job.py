@@ -97,6 +97,8 @@ class ResidentJob:
         self.d_flen = torch.tensor(self.file_lens, dtype=torch.int64, device=dev)
         self.d_first = torch.from_numpy(self.first_row.view(np.int32)).to(dev)
         self.scratch_bytes = self.L.par2cuda_muladd_scratch_bytes(self.R, self.N)
+        if method == _lib.METHOD_TENSOR_FP4:
+            self.scratch_bytes = self.L.par2cuda_tensor_fp4_scratch_bytes(self.R, self.N, self.row_words)
         self.d_scratch = torch.empty(max(self.scratch_bytes, 256), dtype=torch.uint8, device=dev)
         self.d_ck = torch.empty(max(self.N, self.R) * 8, dtype=torch.uint8, device=dev)
         self.d_flags = torch.empty(self.R, dtype=torch.uint8, device=dev)
