@@ -568,7 +568,7 @@ def dense_measure(args, local, steps):
     cfg = WORKLOADS["dense"]
     S, N, R = cfg["S"], cfg["N"], cfg["R"]
     fl = [N * S]
-    job = ResidentJob(S, fl, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.method])
+    job = ResidentJob(S, fl, list(range(R)), device=local, method=_lib.METHOD_NAMES[args.dense_method])
     job.fill_synthetic(seed=7)
     torch.cuda.synchronize()
     r = single_job_measure(args, cfg, fl, job, steps, warmup=3, e2e=not args.no_e2e)
@@ -668,6 +668,19 @@ def roofline_gf(mul_adds, muladd_ms, lop3_ops, n_sm, sm_mhz, kname, alg_bytes):
     return out
 
 
+def roofline_tensor(mul_adds, muladd_ms, mma_macs, kname):
+    """Tensor roofline of the block-scaled 4-bit form: 256 binary
+    multiply-accumulates (512 flops) per word mul-add against the MMA rate of
+    the same instruction measured on this device (par2cuda_tensor_fp4_rate);
+    the call's time includes its two operand-preparation kernels."""
+    flops = mul_adds * 512 / (muladd_ms / 1e3)
+    return {"bound": "tensor", "kernel": kname, "achieved": flops / 1e12, "peak": 2 * mma_macs / 1e12,
+            "unit": "TFLOP/s", "frac": flops / (2 * mma_macs), "traffic": None,
+            "peak_source": "measured: k_tc4_mma_rate, tcgen05.mma kind::mxf4 M=128 N=256 K=64 back to back on "
+                           "shared-memory operands, one CTA per SM (nominal dense fp4 of the part: 13.5 PFLOP/s)",
+            "mul_adds_per_s": mul_adds / (muladd_ms / 1e3), "muladd_ms": muladd_ms}
+
+
 def run_ours(args, cfg, file_lens):
     import torch
     import torch.distributed as dist
@@ -702,6 +715,9 @@ def run_ours(args, cfg, file_lens):
     md5_chain = ctypes.c_double(0)
     if cfg["hashes"]:
         _lib.check(L.par2cuda_md5_chain_rate(ctypes.byref(md5_chain), None), "md5_chain_rate")
+    fp4_rate = ctypes.c_double(0)
+    if "tensor_fp4" in (args.method, args.dense_method):
+        _lib.check(L.par2cuda_tensor_fp4_rate(ctypes.byref(fp4_rate), None), "tensor_fp4_rate")
     torch.cuda.synchronize()
 
     clock_lines, stop = [], threading.Event()
@@ -766,6 +782,7 @@ def run_ours(args, cfg, file_lens):
     rgf = roofline_gf(mul_adds, muladd_ms, lop3.value, n_sm, sm_mhz, kname, alg_bytes)
     if args.traffic_bytes:
         rgf["traffic"] = args.traffic_bytes
+    rtc = roofline_tensor(mul_adds, muladd_ms, fp4_rate.value, kname) if args.method == "tensor_fp4" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -812,15 +829,21 @@ def run_ours(args, cfg, file_lens):
                 "peak_source": "measured: k_md5_chain, one MD5 stream on one thread with its data in registers"}
     # `roofline`: the kernel that takes most of the timed region's device time
     # (the contraction in the job stream and the dense workload)
-    line["roofline"] = dict(rgf)
+    if rtc is not None:
+        line["roofline_tensor"] = rtc
+    line["roofline"] = dict(rtc if rtc is not None else rgf)
     if dense is not None:
         dm = WORKLOADS["dense"]
         d_mul = dm["N"] * dm["R"] * (dm["S"] // 2)
-        dk = _lib.comb_kernel_name(L.par2cuda_comb_shape_for(dm["R"])) if args.method in ("comb", "auto") else kname
-        line["dense"] = {"desc": dm["desc"], "value": dense["value"], "unit": UNIT, "ms_per_step": dense["ms_per_job"],
-                         "steps": dense["jobs"], "e2e": dense.get("e2e"),
+        dkn = {"xor": "k_xor_planes", "nibble": "k_nibble_muladd", "tensor": "k_tc_muladd", "tensor_fp4": "k_tc4_gemm"}
+        dk = _lib.comb_kernel_name(L.par2cuda_comb_shape_for(dm["R"])) if args.dense_method in ("comb", "auto") else \
+            dkn[args.dense_method]
+        line["dense"] = {"desc": dm["desc"], "method": args.dense_method, "value": dense["value"], "unit": UNIT,
+                         "ms_per_step": dense["ms_per_job"], "steps": dense["jobs"], "e2e": dense.get("e2e"),
                          "roofline_gf": roofline_gf(d_mul, dense["muladd_ms"], lop3.value, n_sm, sm_mhz, dk,
                                                     (dm["N"] + dm["R"]) * dm["S"])}
+        if args.dense_method == "tensor_fp4":
+            line["dense"]["roofline_tensor"] = roofline_tensor(d_mul, dense["muladd_ms"], fp4_rate.value, dk)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1)
     print(json.dumps(line))
@@ -1068,6 +1091,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=40.0,
                     help="seconds of CPU work in the reference arm's sample of the batched / serving mix")
     ap.add_argument("--no-dense", action="store_true", help="skip the dense-contraction figure of the default run")
+    ap.add_argument("--dense-method", choices=["comb", "xor", "nibble", "tensor", "tensor_fp4"], default="tensor_fp4",
+                    help="multiply-accumulate kernel of the default run's dense figure")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per comb launch from an ncu capture (profiles/), reported as roofline_gf.traffic")
     args = ap.parse_args()

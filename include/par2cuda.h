@@ -206,6 +206,11 @@ size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in);
  * most 1 GiB of words (more scratch = larger chunks; at least one 128-word
  * tile).  No counterpart in the reference. */
 size_t par2cuda_tensor_fp4_scratch_bytes(unsigned num_rec, unsigned num_in, size_t n_words);
+/* Measures the tensor pipe's rate (binary multiply-accumulates per second)
+ * for the MMA of PAR2CUDA_METHOD_TENSOR_FP4 (M=128, N=256, K=64, mxf4) with one
+ * CTA per SM issuing MMAs on shared-memory operands (about 0.1 s): the
+ * roofline denominator of that method.  No counterpart in the reference. */
+int par2cuda_tensor_fp4_rate(double* macs_per_s, void* stream);
 /* rec[r][0..n_words) (^)= sum_i coeff[r*num_in + i] * in[i][0..n_words),
  * the run_kernel body (gf16/controller_cpu.cpp:488-515).  Pitches are in
  * 16-bit words (even); rows must be readable/writable up to

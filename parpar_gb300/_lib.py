@@ -96,6 +96,7 @@ SIGNATURES = [
     ("par2cuda_file_md5_staged", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _u, _vp]),
     ("par2cuda_copy_rows", _i, [_vp, _sz, _vp, _sz, _sz, _u, _vp]),
     ("par2cuda_tensor_fp4_scratch_bytes", _sz, [_u, _u, _sz]),
+    ("par2cuda_tensor_fp4_rate", _i, [ctypes.POINTER(ctypes.c_double), _vp]),
     ("par2cuda_wait_selftest", _i, [_u, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_double)]),
     ("par2cuda_rows_md5", _i, [_vp, _sz, _u, _sz, _vp, _u, _vp, _vp]),
     ("par2cuda_synth_fill", _i, [_vp, _sz, _u, _sz, _u64, _u64, _vp]),

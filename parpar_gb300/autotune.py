@@ -2,9 +2,9 @@
 
 Method: for each bucket of recovery counts the tuner times every
 multiply-accumulate method of the library (comb XOR-combination tables, the
-LOP3 bit-plane form, split-nibble tables, the tcgen05 tensor-core form) on a
-small resident problem through par2cuda_muladd, and keeps the fastest
-(best_method).
+LOP3 bit-plane form, split-nibble tables, the tcgen05 e4m3 and block-scaled
+4-bit tensor-core forms) on a small resident problem through par2cuda_muladd,
+and keeps the fastest (best_method).
 
 Shape: the comb kernel's cost per word mul-add depends on how many recovery
 rows one CTA serves (the 256-row XOR table is built once per 8 inputs and
@@ -71,7 +71,22 @@ def _time_shape(shape: int, R: int, n: int = 256, slice_bytes: int = 262144, rep
 
 
 METHODS = {"comb": _lib.METHOD_COMB, "xor": _lib.METHOD_XOR, "nibble": _lib.METHOD_NIBBLE,
-           "tensor": _lib.METHOD_TENSOR}
+           "tensor": _lib.METHOD_TENSOR, "tensor_fp4": _lib.METHOD_TENSOR_FP4}
+# word-chunk scratch of the 4-bit tensor method per job (it needs the
+# coefficient bit matrix plus at least one 128-word tile of input planes;
+# more scratch only means fewer, larger chunks)
+FP4_CHUNK_BYTES = 256 << 20
+
+
+def scratch_bytes(method: str, R: int, N: int, n_words: int) -> int:
+    """Scratch par2cuda_muladd needs for `method` on an R x N job."""
+    L = _lib.load()
+    if method == "tensor_fp4":
+        full = L.par2cuda_tensor_fp4_scratch_bytes(R, N, n_words)
+        kbytes = (N + 15) // 16 * 16 * 8
+        bbytes = ((R + 15) // 16 * 16 * 16 * kbytes + 1023) // 1024 * 1024
+        return min(full, bbytes + max(FP4_CHUNK_BYTES, 128 * kbytes))
+    return L.par2cuda_muladd_scratch_bytes(R, N)
 
 
 def _time_method(method: int, R: int, n: int = 256, slice_bytes: int = 262144, reps: int = 3) -> float:
@@ -82,9 +97,10 @@ def _time_method(method: int, R: int, n: int = 256, slice_bytes: int = 262144, r
     _lib.check(L.par2cuda_synth_fill(d_in.data_ptr(), pitch, n, slice_bytes, 98, 0, None), "synth")
     coeff = torch.from_numpy(np.random.default_rng(R + 1).integers(0, 65536, size=(R, n), dtype=np.uint16).view(np.int16)).cuda()
     d_rec = torch.empty((R, pw), dtype=torch.int16, device="cuda")
-    sb = L.par2cuda_muladd_scratch_bytes(R, n)
-    scratch = torch.empty(max(sb, 256), dtype=torch.uint8, device="cuda")
     nw = ((slice_bytes + 7) // 8 * 8 + 8) // 2
+    name = [k for k, v in METHODS.items() if v == method][0]
+    sb = scratch_bytes(name, R, n, nw)
+    scratch = torch.empty(max(sb, 256), dtype=torch.uint8, device="cuda")
 
     def once():
         _lib.check(L.par2cuda_muladd(d_in.data_ptr(), pw, n, coeff.data_ptr(), d_rec.data_ptr(), pw, R, nw, 0,
@@ -104,8 +120,8 @@ def _time_method(method: int, R: int, n: int = 256, slice_bytes: int = 262144, r
 
 
 def best_method(R: int) -> str:
-    """Fastest multiply-accumulate method ("comb", "xor", "nibble" or
-    "tensor") for R recovery rows on this device."""
+    """Fastest multiply-accumulate method ("comb", "xor", "nibble", "tensor"
+    or "tensor_fp4") for R recovery rows on this device."""
     dev = torch.cuda.current_device()
     key = (dev, "method", _bucket(R))
     if key not in _cache:

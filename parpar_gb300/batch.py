@@ -144,8 +144,8 @@ class BatchRunner:
             # scratch of its own (made on the first, eager, call; the resident
             # index bytes stay untouched for the persistent launch)
             if getattr(b, "d_mscratch", None) is None:
-                b.d_mscratch = torch.empty(max(self.L.par2cuda_muladd_scratch_bytes(b.spec.R, b.spec.N), 256),
-                                           dtype=torch.uint8, device=self.dev)
+                sb = autotune.scratch_bytes(method, b.spec.R, b.spec.N, self._n_words(b.W))
+                b.d_mscratch = torch.empty(max(sb, 256), dtype=torch.uint8, device=self.dev)
             _lib.check(self.L.par2cuda_muladd(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_coeff.data_ptr(), b.d_rec.data_ptr(),
                                               b.pw, b.spec.R, self._n_words(n), 0, autotune.METHODS[method],
                                               b.d_mscratch.data_ptr(), b.d_mscratch.numel(), st), "muladd")

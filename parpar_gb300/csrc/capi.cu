@@ -158,6 +158,11 @@ size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in) {
 	return p2c::round_up(std::max(p2c::idx_bytes(num_rec, num_in), p2c::tc_scratch_bytes(num_rec, num_in)), 256);
 }
 
+int par2cuda_tensor_fp4_rate(double* macs_per_s, void* stream) {
+	if(!macs_per_s) { p2c::set_error("tensor_fp4_rate: null output"); return -1; }
+	return p2c::tc4_mma_rate(macs_per_s, (cudaStream_t)stream);
+}
+
 size_t par2cuda_tensor_fp4_scratch_bytes(unsigned num_rec, unsigned num_in, size_t n_words) {
 	return p2c::tc4_scratch_bytes(num_rec, num_in, n_words);
 }

@@ -364,6 +364,95 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 	return 0;
 }
 
+// ------------------------------------------------------------------ peak
+// Calibration of the roofline denominator: one CTA per SM issues `iters`
+// MMAs of the GEMM's shape (M=128, N=256, K=64, kind::mxf4, unit scales) on
+// operands resident in shared memory, back to back into one accumulator, and
+// waits (bounded) for their completion.  No global memory traffic: the rate
+// is the tensor pipe's for this instruction.
+__global__ void __launch_bounds__(128, 1) k_tc4_mma_rate(unsigned iters)
+{
+	extern __shared__ __align__(1024) uint8_t smem_raw[];
+	const uint32_t raw = t4_saddr(smem_raw);
+	const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
+	uint8_t* sm = smem_raw + pad;
+	const uint32_t sbase = raw + pad;
+	const uint32_t doneBar = sbase + T4_STAGE;
+	uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + T4_STAGE + 8);
+	const int warp = threadIdx.x >> 5;
+	for(int e = threadIdx.x; e < T4_STAGE / 16; e += 128) reinterpret_cast<uint4*>(sm)[e] = make_uint4(0, 0, 0, 0);
+	if(threadIdx.x == 0) {
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(doneBar) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+	if(warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(t4_saddr(tslot)), "r"(512u) : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	const uint32_t tmem = *tslot;
+	{
+		const uint32_t one = 0x7F7F7F7Fu;
+		const uint32_t lane0 = (uint32_t)(32 * warp) << 16;
+#pragma unroll
+		for(int q = 0; q < 8; q++)
+			asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+			             "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};"
+			             :: "r"(tmem + lane0 + 256 + 32 * q), "r"(one) : "memory");
+		asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	if(threadIdx.x == 0) {
+		const uint32_t idesc = t4_idesc();
+		const uint64_t ad = t4_desc(sbase), bd = t4_desc(sbase + T4_STAGE_A);
+		for(unsigned it = 0; it < iters; it++) {
+			const uint32_t acc = it != 0;
+			asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
+			             "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], [%5], p;\n\t}"
+			             :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(tmem + 256), "r"(tmem + 384), "r"(acc) : "memory");
+		}
+		asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(doneBar) : "memory");
+	}
+	__syncwarp();
+	t4_wait(doneBar, 0);
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	__syncthreads();
+	if(warp == 0)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(512u) : "memory");
+}
+
+int tc4_mma_rate(double* macsPerSec, cudaStream_t st) {
+	int dev = 0, sms = 0;
+	P2C_CUDA_TRY(cudaGetDevice(&dev));
+	P2C_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	const size_t smem = T4_STAGE + 8 + 16 + 1024;
+	P2C_CUDA_TRY(cudaFuncSetAttribute(k_tc4_mma_rate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const unsigned iters = 20000;
+	cudaEvent_t e0, e1;
+	P2C_CUDA_TRY(cudaEventCreate(&e0));
+	P2C_CUDA_TRY(cudaEventCreate(&e1));
+	float best = 0.f;
+	for(int rep = 0; rep < 3; rep++) {
+		cudaEventRecord(e0, st);
+		k_tc4_mma_rate<<<sms, 128, smem, st>>>(iters);
+		cudaEventRecord(e1, st);
+		cudaEventSynchronize(e1);
+		float ms = 0.f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if(rep == 0 || ms < best) best = ms;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	P2C_CUDA_TRY(cudaGetLastError());
+	*macsPerSec = best > 0.f ? (double)iters * sms * T4_BM * T4_BN * 64 / (best * 1e-3) : 0.0;
+	return 0;
+}
+
 int tc4_error_take() {
 	unsigned v = 0, z = 0;
 	if(cudaMemcpyFromSymbol(&v, g_tc4_error, sizeof(v)) != cudaSuccess) return -1;

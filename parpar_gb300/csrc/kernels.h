@@ -94,4 +94,5 @@ size_t tc4_scratch_bytes(unsigned R, unsigned nIn, size_t nWords);
 int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec, size_t recPitch,
                unsigned R, size_t nWords, int accumulate, void* scratch, size_t scratchBytes, cudaStream_t st);
 int tc4_error_take();
+int tc4_mma_rate(double* macsPerSec, cudaStream_t st);
 } // namespace p2c

@@ -75,6 +75,8 @@ class JobStream:
         self.d_lens = torch.from_numpy(self.row_lens.view(np.int32)).to(dev)
         self.d_coeff = torch.from_numpy(par2_coefficients(np.arange(N), self.exps).view(np.int16)).to(dev)
         self.scratch_bytes = L.par2cuda_muladd_scratch_bytes(R, N)
+        if method == _lib.METHOD_TENSOR_FP4:
+            self.scratch_bytes = L.par2cuda_tensor_fp4_scratch_bytes(R, N, self.row_words)
         self.d_scratch = torch.empty(max(self.scratch_bytes, 256), dtype=torch.uint8, device=dev)
         self.d_ck = torch.empty(max(N, R) * 8, dtype=torch.uint8, device=dev)
         # file MD5 tables of one group: the files of its `group` slots in

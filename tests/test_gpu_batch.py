@@ -120,7 +120,7 @@ def test_batch_descriptors_edge_jobs(shape):
         assert np.array_equal(got, expect)
 
 
-@pytest.mark.parametrize("method", ["xor", "nibble", "tensor"])
+@pytest.mark.parametrize("method", ["xor", "nibble", "tensor", "tensor_fp4"])
 def test_grid_mode_with_each_method_matches_oracle(method):
     """The batched grid path with the autotuner's choice forced to each
     non-comb method (the choice the tuner may make for some recovery count)."""
