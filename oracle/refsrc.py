@@ -1,7 +1,8 @@
 """The reference's own CPU core as a checker — test infrastructure, not product code.
 
 ParPar's gf16/ + hasher/ sources are read from the reference tree named by the
-environment variable PARPAR_REFERENCE (the checkout of Ravencentric/ParPar) and
+environment variable PARPAR_REFERENCE (the checkout of Ravencentric/ParPar;
+default: the read-only checkout at DEFAULT_REFERENCE, when present) and
 staged, unmodified, into oracle/_ref/src/.  That folder is git-ignored: the
 sources never enter the repository's history, but they travel with the working
 tree to the GPU host, which is an aarch64 machine where the x86 objects built
@@ -39,11 +40,15 @@ _SKIP = ("controller_ocl.h", "controller_ocl.cpp", "controller_ocl_init.cpp", "x
 _SRC_HEADERS = ("platform.h", "cpuid.h", "hedley.h", "stdint.h")
 
 
+DEFAULT_REFERENCE = "/root/reference"
+
+
 def reference_dir() -> str | None:
-    """The reference checkout named by PARPAR_REFERENCE, if it holds gf16/."""
-    d = os.environ.get("PARPAR_REFERENCE")
-    if d and os.path.isfile(os.path.join(d, "gf16", "controller.h")):
-        return d
+    """The reference checkout named by PARPAR_REFERENCE (else the read-only
+    checkout at DEFAULT_REFERENCE), if it holds gf16/."""
+    for d in (os.environ.get("PARPAR_REFERENCE"), DEFAULT_REFERENCE):
+        if d and os.path.isfile(os.path.join(d, "gf16", "controller.h")):
+            return d
     return None
 
 

@@ -143,6 +143,15 @@ int Engine::alloc_desc() {
 	return 0;
 }
 
+size_t Engine::fp4_scratch_bytes() const {
+	// the coefficient bit matrix of a full batch plus word chunks of at most
+	// 512 MiB of expanded input planes
+	const size_t kBytes = round_up(batchPad, 16) * 8;
+	const size_t bBytes = round_up(round_up(std::max<size_t>(outputExponents.size(), 1), 16) * 16 * kBytes, 1024);
+	return std::min(tc4_scratch_bytes((unsigned)outputExponents.size(), batchPad, row_words(allocSliceSize)),
+	                bBytes + std::max<size_t>(512ull << 20, 128 * kBytes));
+}
+
 int Engine::alloc_processing() {
 	P2C_CUDA_TRY(cudaSetDevice(device));
 	size_t R = outputExponents.size();
@@ -162,6 +171,8 @@ int Engine::alloc_processing() {
 	size_t need = round_up(std::max(idx_bytes((unsigned)R, batchPad), tc_scratch_bytes((unsigned)R, batchPad)), 256) +
 	              round_up(R * batchPad * 2, 256) +
 	              round_up(std::max<size_t>(R, batchPad) * 8, 256) + round_up(R, 256);
+	// the 4-bit tensor method's operand planes follow (method 5 only)
+	if(method == 5) need += fp4_scratch_bytes();
 	if(need > scratchBytes) {
 		if(dScratch) cudaFree(dScratch);
 		dScratch = nullptr;
@@ -175,7 +186,7 @@ int Engine::alloc_processing() {
 int Engine::init(int m, unsigned inputBatch) {
 	if(!sliceSize) { set_error("setSliceSize must be called before init"); return -1; }
 	method = m == 0 ? 1 : m;
-	if(method < 1 || method > 4) { set_error("unknown method %d", m); return -1; }
+	if(method < 1 || method > 5) { set_error("unknown method %d", m); return -1; }
 	inputBatchSize = inputBatch ? inputBatch : (unsigned)default_batch(sliceSize);
 	if(inputBatchSize > 32768) { set_error("input batch size %u > 32768", inputBatchSize); return -1; }
 	batchPad = (unsigned)round_up(inputBatchSize, 8);
@@ -193,6 +204,13 @@ int Engine::init(int m, unsigned inputBatch) {
 		// later init succeeds
 		free_staging();
 		initialised = false;
+		return -1;
+	}
+	// a new method or batch size changes the scratch that recovery rows
+	// already set need
+	if(!outputExponents.empty() && alloc_processing()) {
+		free_processing();
+		outputExponents.clear();
 		return -1;
 	}
 	return 0;
@@ -576,6 +594,11 @@ int Engine::run_kernel(unsigned areaIdx, unsigned numInputs) {
 	else if(method == 3) rc = nibble_muladd_t(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, gt, sCompute);
 	else if(method == 4) rc = tc_muladd(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, true, dIdx,
 	                                    tc_scratch_bytes(R, numInputs), sCompute);
+	else if(method == 5) {
+		uint8_t* fp = reinterpret_cast<uint8_t*>(dScratch) + (scratchBytes - fp4_scratch_bytes());
+		rc = tc4_muladd(a.dIn, pitch, numInputs, dCoeff, dRec, recPitchAlloc, R, nWords, acc, fp, fp4_scratch_bytes(),
+		                sCompute);
+	}
 	else rc = comb_muladd(a.dIn, pitch, numInputs, dIdx, dRec, recPitchAlloc, R, nWords, acc, shape, sCompute);
 	if(rc) return -1;
 	processingAdd = true;
@@ -659,8 +682,8 @@ int Engine::info(par2cuda_info* o) {
 	cudaDeviceProp p;
 	if(cudaGetDeviceProperties(&p, device) == cudaSuccess) snprintf(o->device_name, sizeof(o->device_name), "%.127s", p.name);
 	const char* names[] = {"auto", "Comb (XOR-combination tables)", "Xor (LOP3 bit masks)", "Nibble tables",
-	                       "Tensor (tcgen05 GF(2) bit-matrix, e4m3)"};
-	snprintf(o->method_desc, sizeof(o->method_desc), "%s", names[method >= 0 && method <= 4 ? method : 0]);
+	                       "Tensor (tcgen05 GF(2) bit-matrix, e4m3)", "Tensor (tcgen05 GF(2) bit-matrix, block-scaled e2m1)"};
+	snprintf(o->method_desc, sizeof(o->method_desc), "%s", names[method >= 0 && method <= 5 ? method : 0]);
 	o->staging_count = (unsigned)staging.size();
 	o->staging_size = inputBatchSize;
 	o->min_staging_size = minInBatchSize;

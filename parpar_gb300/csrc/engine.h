@@ -115,6 +115,7 @@ private:
 	int alloc_staging();
 	int alloc_desc();
 	int alloc_processing();
+	size_t fp4_scratch_bytes() const;
 	void free_staging();
 	void free_processing();
 	void wait_idle();

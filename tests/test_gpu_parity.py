@@ -19,7 +19,7 @@ from parpar_gb300.gfproc import GfProc, GfProcError, create_recovery
 
 pytestmark = pytest.mark.gpu
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
-METHODS = ["comb", "xor", "nibble", "tensor"]
+METHODS = ["comb", "xor", "nibble", "tensor", "tensor_fp4"]
 
 
 def golden_inputs(c):
