@@ -36,6 +36,10 @@ import time
 
 import numpy as np
 
+# enough hardware queues for the job stream's concurrent streams; must be set
+# before the CUDA context exists (parpar_gb300/__init__.py explains why)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -549,9 +553,14 @@ def stream_measure(args, cfg, file_lens, local, rank, barrier, max_over_ranks):
                       "d2h_bytes_per_step": js.d2h_bytes(), "ms_per_step": ems,
                       "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                       "h2d_GBps_one_job": h2d_gbps,
-                      "path": "par2cuda C ABI, job stream: per job one 2-D H2D of its slices from pinned host memory "
-                              "into its slot, the job's kernels, one D2H of recovery + IFSC + file MD5 + verdicts into "
-                              "pinned host buffers; %d slots, file MD5s pooled per %d jobs" % (js.slots, js.group)}
+                      "h2d_GBps_in_stream": (args.steps * N * S / (js.upload_span_ms() / 1e3) / 1e9
+                                             if js.upload_span_ms() else None),
+                      "size_classes": [len(c) for c in js.classes],
+                      "path": "par2cuda C ABI, job stream: each job's slices copied from pinned host memory into "
+                              "its slot by 2-D H2D copies (files in size classes, largest first across the jobs in flight; each "
+                              "class's file MD5 launch per group starts when its rows have landed), the job's kernels, "
+                              "one D2H of recovery + IFSC + file MD5 + verdicts into pinned host buffers; %d slots, "
+                              "file MD5s pooled per %d jobs" % (js.slots, js.group)}
         del host_in, host_out
     del js
     torch.cuda.empty_cache()

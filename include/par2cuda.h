@@ -282,6 +282,15 @@ int par2cuda_rows_md5(const void* d_rows, size_t pitch_bytes, unsigned num_rows,
 int par2cuda_file_md5_staged(const void* d_rows, size_t pitch_bytes, unsigned num_files, const uint64_t* d_file_len,
                              const uint32_t* d_first_row, size_t slice_bytes, uint8_t* d_md5, unsigned files_per_block,
                              void* stream);
+/* par2cuda_file_md5_staged over any subset of files, in any order: table
+ * entry f's digest is written to d_md5 + 16 * d_out_index[f] (to d_md5 +
+ * 16 * f when d_out_index is NULL).  A job stream hashes its largest files
+ * first, as soon as their rows have landed, and the rest later, each digest
+ * in its file's place.  No counterpart in the reference. */
+int par2cuda_file_md5_staged_indexed(const void* d_rows, size_t pitch_bytes, unsigned num_files,
+                                     const uint64_t* d_file_len, const uint32_t* d_first_row,
+                                     const uint32_t* d_out_index, size_t slice_bytes, uint8_t* d_md5,
+                                     unsigned files_per_block, void* stream);
 /* Copies num_rows rows of row_bytes bytes between host and device memory (or
  * within either) with one 2-D copy on `stream`: the H2D of input slices into
  * the backend's pitched rows, the D2H of recovery rows into packed host

@@ -94,6 +94,7 @@ SIGNATURES = [
     ("par2cuda_file_md5_packed", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _vp]),
     ("par2cuda_file_md5_pooled", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _u, _vp]),
     ("par2cuda_file_md5_staged", _i, [_vp, _sz, _u, _vp, _vp, _sz, _vp, _u, _vp]),
+    ("par2cuda_file_md5_staged_indexed", _i, [_vp, _sz, _u, _vp, _vp, _vp, _sz, _vp, _u, _vp]),
     ("par2cuda_copy_rows", _i, [_vp, _sz, _vp, _sz, _sz, _u, _vp]),
     ("par2cuda_tensor_fp4_scratch_bytes", _sz, [_u, _u, _sz]),
     ("par2cuda_tensor_fp4_rate", _i, [ctypes.POINTER(ctypes.c_double), _vp]),

@@ -246,6 +246,13 @@ int par2cuda_file_md5_staged(const void* d_rows, size_t pitch_bytes, unsigned nu
 	return p2c::file_md5_staged(d_rows, pitch_bytes, num_files, d_file_len, d_first_row, slice_bytes, d_md5,
 	                            files_per_block, (cudaStream_t)stream);
 }
+int par2cuda_file_md5_staged_indexed(const void* d_rows, size_t pitch_bytes, unsigned num_files,
+                                     const uint64_t* d_file_len, const uint32_t* d_first_row,
+                                     const uint32_t* d_out_index, size_t slice_bytes, uint8_t* d_md5,
+                                     unsigned files_per_block, void* stream) {
+	return p2c::file_md5_staged(d_rows, pitch_bytes, num_files, d_file_len, d_first_row, slice_bytes, d_md5,
+	                            files_per_block, (cudaStream_t)stream, d_out_index);
+}
 int par2cuda_copy_rows(void* dst, size_t dst_pitch, const void* src, size_t src_pitch, size_t row_bytes,
                        unsigned num_rows, void* stream) {
 	if(!num_rows || !row_bytes) return 0;

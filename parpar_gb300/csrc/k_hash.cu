@@ -419,7 +419,7 @@ template<int NT>
 __global__ void __launch_bounds__(NT) k_file_md5_staged(const uint8_t* __restrict__ rows, size_t pitch, unsigned nFiles,
                                                         const uint64_t* __restrict__ fileLen,
                                                         const uint32_t* __restrict__ firstRow, size_t sliceBytes,
-                                                        uint8_t* __restrict__ out)
+                                                        uint8_t* __restrict__ out, const uint32_t* __restrict__ outIndex)
 {
 	extern __shared__ __align__(128) uint8_t smem[];
 	const unsigned t = threadIdx.x;
@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(NT) k_file_md5_staged(const uint8_t* __restric
 		return;
 	}
 	md5_finish(st, tail, tailLen, 0, total);
-	uint8_t* o = out + (size_t)f * 16;
+	uint8_t* o = out + (size_t)(outIndex ? outIndex[f] : f) * 16;
 #pragma unroll
 	for(int w = 0; w < 4; w++) {
 		o[4 * w] = (uint8_t)st[w]; o[4 * w + 1] = (uint8_t)(st[w] >> 8);
@@ -528,7 +528,8 @@ __global__ void __launch_bounds__(NT) k_file_md5_staged(const uint8_t* __restric
 }
 
 int file_md5_staged(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen,
-                    const uint32_t* dFirstRow, size_t sliceBytes, uint8_t* dOut, unsigned filesPerBlock, cudaStream_t st)
+                    const uint32_t* dFirstRow, size_t sliceBytes, uint8_t* dOut, unsigned filesPerBlock, cudaStream_t st,
+                    const uint32_t* dOutIndex)
 {
 	if(!nFiles) return 0;
 	if(pitchBytes % 16 || ((uintptr_t)rows & 15)) { set_error("staged file MD5: rows must be 16-byte aligned"); return -1; }
@@ -538,11 +539,11 @@ int file_md5_staged(const void* rows, size_t pitchBytes, unsigned nFiles, const 
 	if(filesPerBlock == 32) {
 		P2C_CUDA_TRY(cudaFuncSetAttribute(k_file_md5_staged<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 		k_file_md5_staged<32><<<(nFiles + 31) / 32, 32, smem, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen,
-		                                                             dFirstRow, sliceBytes, dOut);
+		                                                             dFirstRow, sliceBytes, dOut, dOutIndex);
 	} else {
 		P2C_CUDA_TRY(cudaFuncSetAttribute(k_file_md5_staged<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 		k_file_md5_staged<64><<<(nFiles + 63) / 64, 64, smem, st>>>((const uint8_t*)rows, pitchBytes, nFiles, dFileLen,
-		                                                             dFirstRow, sliceBytes, dOut);
+		                                                             dFirstRow, sliceBytes, dOut, dOutIndex);
 	}
 	P2C_CUDA_TRY(cudaGetLastError());
 	return 0;

@@ -85,9 +85,11 @@ int synth_fill(void* dst, size_t pitchBytes, unsigned nRows, size_t rowBytes, ui
 // bounded-wait self-test (k_comb.cu): a wait that nothing completes gives up
 // after `polls` polls and sets the multiply-accumulate error flag
 int wait_selftest(unsigned polls, int* gaveUp, double* seconds);
-// file MD5 with each chain's bytes staged into shared memory by bulk copies
+// file MD5 with each chain's bytes staged into shared memory by bulk copies;
+// table entry f's digest goes to dOut + 16 * dOutIndex[f] (f when null)
 int file_md5_staged(const void* rows, size_t pitchBytes, unsigned nFiles, const uint64_t* dFileLen,
-                    const uint32_t* dFirstRow, size_t sliceBytes, uint8_t* dOut, unsigned filesPerBlock, cudaStream_t st);
+                    const uint32_t* dFirstRow, size_t sliceBytes, uint8_t* dOut, unsigned filesPerBlock, cudaStream_t st,
+                    const uint32_t* dOutIndex = nullptr);
 int hash_error_take();
 // block-scaled 4-bit tcgen05 form (k_tc4.cu)
 size_t tc4_scratch_bytes(unsigned R, unsigned nIn, size_t nWords);

@@ -21,7 +21,16 @@ shape (slice size, file lengths, recovery exponents):
 With host buffers (run(..., host_in=..., host_out=...)) every job's inputs are
 copied to its slot on a copy stream and its results (recovery slices, IFSC
 entries, file MD5s, verdicts) copied back on a download stream; a slot is
-refilled only after every read of its previous job is done.
+refilled only after every read of its previous job is done.  The copies of a
+window of jobs go largest files first: the files are split into size classes
+(`size_classes`, fractions of the largest file's length), and the rows of
+class 0 of the window's jobs land before those of class 1, and so on, in a
+staircase (upload_order) that also lands the first jobs whole early.
+Each class of a group has its own file MD5 launch (par2cuda_file_md5_staged_
+indexed, digests in their files' places), started as soon as that class's
+rows of the group have landed, so the longest chains start within the first
+few percent of the copies instead of after the whole window; a job's
+contraction starts once its last class has landed.
 
 Every job's work is exactly the single-job path's (parpar_gb300.job), through
 the same C-ABI entry points; the PAR2 semantics follow lib/par2gen.js's
@@ -39,7 +48,8 @@ from .layout import file_layout
 
 class JobStream:
     def __init__(self, slice_size: int, file_lens, exps, slots: int = 24, group: int = 8, device: int = 0,
-                 method: int = _lib.METHOD_COMB, md5_block: int = 64, md5_staged: bool = True):
+                 method: int = _lib.METHOD_COMB, md5_block: int = 64, md5_staged: bool = True,
+                 size_classes=(0.9, 0.75)):
         if slots % group:
             raise ValueError("slots must be a multiple of group")
         L = self.L = _lib.load()
@@ -85,20 +95,53 @@ class JobStream:
         gfirst = np.concatenate([self.first_row.astype(np.int64) + j * N for j in range(group)]).astype(np.uint32)
         self.d_gfirst = torch.from_numpy(gfirst.view(np.int32)).to(dev)
         ng = slots // group
+        # size classes of the files for copies from host buffers: class c
+        # holds the files of length >= size_classes[c] x the largest (and
+        # below the previous bound); empty classes are dropped
+        bounds = sorted((float(t) for t in size_classes), reverse=True) if self.md5_staged else []
+        mx = max(self.file_lens) if F else 0
+        cls = [sum(1 for t in bounds if n < t * mx) for n in self.file_lens]
+        self.classes = [c for c in ([f for f in range(F) if cls[f] == k] for k in range(len(bounds) + 1)) if c]
+        nrows = np.diff(np.append(self.first_row.astype(np.int64), N))
+        self.class_runs, self.class_tables = [], []
+        for files in self.classes:
+            # row runs to copy: consecutive files of the class merged
+            runs = []
+            for f in files:
+                r0, nr = int(self.first_row[f]), int(nrows[f])
+                if runs and runs[-1][0] + runs[-1][1] == r0:
+                    runs[-1][1] += nr
+                else:
+                    runs.append([r0, nr])
+            self.class_runs.append(runs)
+            # file MD5 table of the class for a whole group: lengths, first
+            # rows and digest places counted from the group's first slot
+            lens = np.array([self.file_lens[f] for _ in range(group) for f in files], dtype=np.int64)
+            first = np.array([int(self.first_row[f]) + j * N for j in range(group) for f in files], dtype=np.uint32)
+            out = np.array([j * F + f for j in range(group) for f in files], dtype=np.uint32)
+            self.class_tables.append(tuple(torch.from_numpy(a.view(np.int64 if a.dtype == np.int64 else np.int32)).to(dev)
+                                           for a in (lens, first, out)))
         self.s_comp = torch.cuda.Stream(device=dev)
         self.s_ifsc = [torch.cuda.Stream(device=dev) for _ in range(ng)]
         self.s_md5 = [torch.cuda.Stream(device=dev, priority=-10) for _ in range(ng)]
+        # one more MD5 stream per group for each further size class, so that
+        # the classes' chains run side by side
+        self.s_md5c = [[self.s_md5[g]] + [torch.cuda.Stream(device=dev, priority=-10)
+                                          for _ in range(len(self.classes) - 1)] for g in range(ng)]
         self.s_up = torch.cuda.Stream(device=dev)
         self.s_down = torch.cuda.Stream(device=dev)
         # reads of a slot's rows that must finish before the slot is refilled,
         # and the download of its results before they are overwritten
         self.ev_gf = [None] * slots
         self.ev_ifsc = [None] * slots
-        self.ev_md5 = [None] * ng
+        # per group, the last file MD5 launch on each of its MD5 streams (each
+        # stream runs in order, so these cover every launch still reading
+        # the group's slots)
+        self.ev_md5 = [[None] * len(self.classes or [0]) for _ in range(ng)]
         self.ev_down = [None] * slots
-        self.ev_up = [None] * slots
         self.launches = 0
         self.jobs_done = []
+        self._up_span = None
 
     # ---------------------------------------------------------------- setup
     def fill_synthetic(self, seed0: int):
@@ -125,27 +168,151 @@ class JobStream:
         (rec [R, S], ifsc [N*20], fmd5 [F*16], flags [R]) of pinned uint8
         tensors, job k writing host_out[k % len].  timing=True records events
         for per-job latencies (latencies())."""
-        L, N, R, G = self.L, self.N, self.R, self.group
         cur = torch.cuda.current_stream(self.dev)
-        for st in [self.s_comp, self.s_up, self.s_down] + self.s_ifsc + self.s_md5:
+        streams = [self.s_comp, self.s_up, self.s_down] + self.s_ifsc + [st for c in self.s_md5c for st in c]
+        for st in streams:
             st.wait_stream(cur)
+        self._up_span = None
+        if timing and host_in is not None:
+            self._up_span = [self._event(self.s_up, True), None]
         k = first_job
         end = first_job + count
-        while k < end:
-            g = (k % self.slots) // G
-            n_in_group = min(G - (k % self.slots) % G, end - k)
-            jobs = list(range(k, k + n_in_group))
-            for j in jobs:
-                self._issue_gf(j, host_in, timing)
-            self._issue_md5(g, jobs, timing)
-            if host_out is not None:
+        if host_in is not None and len(self.classes) > 1:
+            # windows of at most `slots` jobs: no slot holds two jobs of a window
+            while k < end:
+                n = min(self.slots, end - k)
+                self._run_window(list(range(k, k + n)), host_in, host_out, timing)
+                k += n
+        else:
+            for g, jobs in self._chunks(k, end):
+                landed = {}
                 for j in jobs:
-                    self._issue_download(j, host_out)
-            k += n_in_group
-        for st in [self.s_comp, self.s_up, self.s_down] + self.s_ifsc + self.s_md5:
+                    landed[j] = self._upload_whole(j, host_in)
+                    self._issue_gf(j, timing, landed[j])
+                self._issue_md5(g, jobs, timing, landed)
+                if host_out is not None:
+                    for j in jobs:
+                        self._issue_download(j, host_out)
+        if self._up_span is not None:
+            self._up_span[1] = self._event(self.s_up, True)
+        for st in streams:
             cur.wait_stream(st)
 
-    def _issue_gf(self, k, host_in, timing):
+    def _chunks(self, k, end):
+        """(group, consecutive jobs of that group) for jobs k .. end-1."""
+        out = []
+        while k < end:
+            g = (k % self.slots) // self.group
+            n = min(self.group - (k % self.slots) % self.group, end - k)
+            out.append((g, list(range(k, k + n))))
+            k += n
+        return out
+
+    def _slot_free(self, stream, k):
+        """`stream` waits until every read of slot k % slots by its previous job
+        is done and that job's results have been copied out."""
+        s = k % self.slots
+        for ev in [self.ev_gf[s], self.ev_ifsc[s], self.ev_down[s]] + self.ev_md5[s // self.group]:
+            self._wait(stream, ev)
+
+    def _upload_whole(self, k, host_in):
+        """All rows of job k in one 2-D copy (no size classes); returns the
+        event of their landing (None for resident rows)."""
+        if host_in is None:
+            return None
+        s = k % self.slots
+        up = self.s_up
+        self._slot_free(up, k)
+        src = host_in[k % len(host_in)]
+        _lib.check(self.L.par2cuda_copy_rows(self.d_in[s * self.N].data_ptr(), self.pitch, src.data_ptr(), self.S,
+                                             self.S, self.N, up.cuda_stream), "h2d")
+        return self._event(up)
+
+    @staticmethod
+    def upload_order(n, classes):
+        """(job index in the window, size class) in copy order: a staircase
+        that lands job 0 whole, then class 0 of every other job, then the rest
+        of job 1, class 1 of jobs 2.., the rest of job 2, and so on; the
+        largest files' MD5 chains start within the first copies while the
+        contraction of the first jobs need not wait for the whole window."""
+        order, done = [], set()
+
+        def add(i, c):
+            if (i, c) not in done:
+                done.add((i, c))
+                order.append((i, c))
+        for c in range(classes):
+            add(0, c)
+        for c in range(classes):
+            for i in range(c + 1, n):
+                add(i, c)
+            if c + 1 < n:
+                for cc in range(c + 1, classes):
+                    add(c + 1, cc)
+        return order
+
+    def _run_window(self, jobs, host_in, host_out, timing):
+        """Copies by size class in upload_order(), each class's file MD5 launch
+        per group as soon as that class of the group's jobs has landed, each
+        job's kernels once its last class has landed."""
+        up, S, N = self.s_up, self.S, self.N
+        C = len(self.classes)
+        chunks = self._chunks(jobs[0], jobs[-1] + 1)
+        chunk_of = {k: ci for ci, (_, cj) in enumerate(chunks) for k in cj}
+        waiting = {(c, ci): len(cj) for c in range(C) for ci, (_, cj) in enumerate(chunks)}
+        left = {k: C for k in jobs}
+        for k in jobs:
+            self._slot_free(up, k)
+        md5_evs = {k: [] for k in jobs}
+        md5_t0 = {}
+        for i, c in self.upload_order(len(jobs), C):
+            k = jobs[i]
+            s = k % self.slots
+            src = host_in[k % len(host_in)].data_ptr()
+            base = self.d_in[s * N].data_ptr()
+            for r0, nr in self.class_runs[c]:
+                _lib.check(self.L.par2cuda_copy_rows(base + r0 * self.pitch, self.pitch, src + r0 * S, S, S, nr,
+                                                     up.cuda_stream), "h2d")
+            left[k] -= 1
+            if not left[k]:
+                self._issue_gf(k, timing, self._event(up))
+            ci = chunk_of[k]
+            waiting[c, ci] -= 1
+            if not waiting[c, ci]:
+                g, cj = chunks[ci]
+                t0, ev = self._issue_md5_class(g, cj, c, self._event(up), timing)
+                for kk in cj:
+                    md5_evs[kk].append(ev)
+                    md5_t0.setdefault(kk, t0)
+        for rec in self.jobs_done[-len(jobs):]:
+            rec["md5"] = md5_evs[rec["job"]]
+            if timing:
+                rec["md5_start"] = md5_t0[rec["job"]]
+        if host_out is not None:
+            for k in jobs:
+                self._issue_download(k, host_out)
+
+    def _issue_md5_class(self, g, jobs, c, ev_landed, timing):
+        """The file MD5 launch of size class c for `jobs` (consecutive slots of group g)."""
+        st = self.s_md5c[g][c]
+        st.wait_event(ev_landed)
+        s0 = jobs[0] % self.slots
+        lens, first, out = self.class_tables[c]
+        nf = len(jobs) * len(self.classes[c])
+        t0 = self._event(st, True) if timing else None
+        _lib.check(self.L.par2cuda_file_md5_staged_indexed(self.d_in[s0 * self.N].data_ptr(), self.pitch, nf,
+                                                           lens.data_ptr(), first.data_ptr(), out.data_ptr(), self.S,
+                                                           self.d_fmd5[s0].data_ptr(), self.md5_block, st.cuda_stream),
+                   "file_md5")
+        ev = self._event(st, timing)
+        self.ev_md5[g][c] = ev
+        self.launches += 1
+        return t0, ev
+
+    def _issue_gf(self, k, timing, landed=None):
+        """Job k's kernels: checksum, contraction and verification on the
+        compute stream, IFSC on its group's side stream; with host buffers
+        they wait for the job's rows to have landed (event `landed`)."""
         L, N, R = self.L, self.N, self.R
         s = k % self.slots
         g = s // self.group
@@ -153,20 +320,12 @@ class JobStream:
         d_in = self.d_in[s * N].data_ptr()
         d_rec = self.d_rec[s * R].data_ptr()
         rec = {"job": k}
-        if host_in is not None:
-            up = self.s_up
-            # the slot's previous job has read its rows and its results have
-            # been copied out before new rows land
-            for ev in (self.ev_gf[s], self.ev_ifsc[s], self.ev_md5[g], self.ev_down[s]):
-                self._wait(up, ev)
-            src = host_in[k % len(host_in)]
-            _lib.check(L.par2cuda_copy_rows(d_in, self.pitch, src.data_ptr(), self.S, self.S, N, up.cuda_stream), "h2d")
-            ev_up = self._event(up)
-            self.ev_up[s] = ev_up
-            comp.wait_event(ev_up)
-            side.wait_event(ev_up)
-        else:
-            self._wait(comp, self.ev_down[s])
+        # the slot's previous results have been copied out (their copy came
+        # before this job's rows were copied in, when there is one)
+        self._wait(comp, self.ev_down[s])
+        if landed is not None:
+            comp.wait_event(landed)
+            side.wait_event(landed)
         if timing:
             rec["start"] = self._event(comp, True)
         a = comp.cuda_stream
@@ -189,7 +348,7 @@ class JobStream:
         rec["gf"], rec["ifsc"] = self.ev_gf[s], self.ev_ifsc[s]
         self.jobs_done.append(rec)
 
-    def _issue_md5(self, g, jobs, timing):
+    def _issue_md5(self, g, jobs, timing, landed):
         """One pooled launch for the file MD5s of `jobs` (consecutive slots of group g)."""
         s0 = jobs[0] % self.slots
         st = self.s_md5[g]
@@ -197,7 +356,7 @@ class JobStream:
         # slots' previous jobs have been copied out
         for j in jobs:
             s = j % self.slots
-            self._wait(st, self.ev_up[s])
+            self._wait(st, landed.get(j))
             self._wait(st, self.ev_down[s])
         j0 = s0 - g * self.group
         nf = len(jobs) * self.F
@@ -208,10 +367,10 @@ class JobStream:
                        self.d_gfirst.data_ptr(), self.S, self.d_fmd5[s0].data_ptr(), self.md5_block, st.cuda_stream),
                    "file_md5")
         ev = self._event(st, timing)
-        self.ev_md5[g] = ev
+        self.ev_md5[g][0] = ev
         self.launches += 1
         for rec in self.jobs_done[-len(jobs):]:
-            rec["md5"] = ev
+            rec["md5"] = [ev]
             if timing:
                 rec["md5_start"] = t0
 
@@ -219,7 +378,7 @@ class JobStream:
         s = k % self.slots
         g = s // self.group
         d = self.s_down
-        for ev in (self.ev_gf[s], self.ev_ifsc[s], self.ev_md5[g]):
+        for ev in [self.ev_gf[s], self.ev_ifsc[s]] + self.ev_md5[g]:
             self._wait(d, ev)
         rec_h, ifsc_h, fmd5_h, flags_h = host_out[k % len(host_out)]
         L, ds = self.L, d.cuda_stream
@@ -238,7 +397,8 @@ class JobStream:
             if "start" not in rec:
                 continue
             start = rec["start"]
-            t_end = max(start.elapsed_time(rec["gf"]), start.elapsed_time(rec["ifsc"]), start.elapsed_time(rec["md5"]))
+            t_end = max([start.elapsed_time(rec["gf"]), start.elapsed_time(rec["ifsc"])] +
+                        [start.elapsed_time(e) for e in rec["md5"]])
             t_beg = min(0.0, start.elapsed_time(rec["md5_start"]))
             out.append((t_end - t_beg) / 1e3)
         return out
@@ -247,6 +407,28 @@ class JobStream:
         """Mean device time of the timed jobs' multiply-accumulate launches (ms)."""
         t = [r["mul0"].elapsed_time(r["mul1"]) for r in self.jobs_done if "mul0" in r]
         return float(np.mean(t)) if t else 0.0
+
+    def upload_span_ms(self):
+        """Milliseconds from the copy stream's start to its last copy of the
+        last timed run with host buffers (0 when it read resident rows)."""
+        if not self._up_span or self._up_span[1] is None:
+            return 0.0
+        return self._up_span[0].elapsed_time(self._up_span[1])
+
+    def timeline(self, t0):
+        """Per timed job, milliseconds from event t0 to each recorded event
+        (upload, contraction, IFSC, file MD5 start and end)."""
+        out = []
+        for r in self.jobs_done:
+            if "start" not in r:
+                continue
+            d = {"job": r["job"]}
+            for k in ("start", "mul0", "mul1", "gf", "ifsc", "md5_start"):
+                if k in r:
+                    d[k] = t0.elapsed_time(r[k])
+            d["md5"] = [t0.elapsed_time(e) for e in r["md5"]]
+            out.append(d)
+        return out
 
     def clear_records(self):
         self.jobs_done = []

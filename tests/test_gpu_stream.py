@@ -133,3 +133,75 @@ def test_staged_file_md5_against_oracle_odd_lengths():
         a = int(first[f])
         data = x[a:a + max(1, -(-ln // S))].reshape(-1)[:ln]
         assert got[f].tobytes() == O.md5(data), ln
+
+
+def test_stream_size_classes_and_mixed_runs():
+    """Three size classes of copies from host buffers (neighbouring files of
+    a class copied together), windows that reuse
+    slots, and resident runs in between on the rows the copies left."""
+    from parpar_gb300.stream import JobStream
+    js = JobStream(S, FILE_LENS, EXPS, slots=4, group=2, size_classes=(0.95, 0.5))
+    assert js.classes == [[3], [0], [1, 2, 4, 5]]
+    assert js.class_runs[2] == [[6, 4], [18, 4]]   # files 1+2 and 4+5: neighbouring rows merged
+    hosts = [torch.from_numpy(synth.slices(90 + k, 0, js.N, S)).pin_memory() for k in range(3)]
+    outs = js.host_out_buffers(5)
+    js.run(6, first_job=0, host_in=hosts, host_out=outs, timing=True)   # windows of 4 + 2 jobs
+    torch.cuda.synchronize()
+    assert js.upload_span_ms() > 0 and len(js.latencies()) == 6
+    js.run(2, first_job=6)                                              # resident, slots 2 and 3
+    js.run(3, first_job=8, host_in=hosts, host_out=outs)                # slots 0, 1, 2
+    torch.cuda.synchronize()
+    want = [expected(h.numpy()) for h in hosts]
+    for k, o in ((1, outs[1]), (2, outs[2]), (8, outs[3]), (9, outs[4]), (10, outs[0])):
+        rec, ifsc, fmd5 = want[k % 3]
+        assert o[3].numpy().all(), k
+        assert np.array_equal(o[0].numpy(), rec), k
+        assert o[1].numpy().tobytes() == ifsc, k
+        assert o[2].numpy().tobytes() == fmd5, k
+    # slot 3 ran job 7 on the rows job 3 copied in (hosts[0]); slot 2 ran job 10 (hosts[1])
+    for s, h in ((3, 0), (2, 1)):
+        rec, ifsc, fmd5 = want[h]
+        got_rec, got_ifsc, got_fmd5, flags = js.slot_results(s)
+        assert flags.all() and np.array_equal(got_rec, rec)
+        assert got_ifsc.tobytes() == ifsc and got_fmd5.tobytes() == fmd5
+
+
+def test_indexed_file_md5_places_digests():
+    """par2cuda_file_md5_staged_indexed over a permuted subset of files puts
+    each digest in its file's place; a null index is the plain staged form."""
+    from parpar_gb300 import _lib
+    L = _lib.load()
+    first, lens = file_layout(FILE_LENS * 5, S)
+    N = len(lens)
+    pitch = L.par2cuda_row_pitch_bytes(S)
+    d = torch.empty((N, pitch), dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    _lib.check(L.par2cuda_synth_fill(d.data_ptr(), pitch, N, S, 11, 0, st), "synth")
+    nf = len(FILE_LENS) * 5
+    flen_all = np.array(FILE_LENS * 5, dtype=np.int64)
+    ref = torch.zeros(nf * 16, dtype=torch.uint8, device="cuda")
+    # device tables held in names: a pointer taken from a temporary tensor
+    # would outlive its memory
+    flen = torch.from_numpy(flen_all).cuda()
+    fr = torch.from_numpy(first.view(np.int32)).cuda()
+    _lib.check(L.par2cuda_file_md5_staged_indexed(d.data_ptr(), pitch, nf, flen.data_ptr(), fr.data_ptr(), None, S,
+                                                 ref.data_ptr(), 64, st), "indexed")
+    x = synth.slices(11, 0, N, S)
+    for f in range(nf):
+        a, ln = int(first[f]), int(flen_all[f])
+        assert ref[16 * f:16 * f + 16].cpu().numpy().tobytes() == O.md5(x[a:a + max(1, -(-ln // S))].reshape(-1)[:ln])
+    rng = np.random.default_rng(4)
+    pick = rng.permutation(nf)[: nf - 7]            # a subset, in shuffled order
+    out = torch.full((nf * 16,), 0xAB, dtype=torch.uint8, device="cuda")
+    tl = torch.from_numpy(flen_all[pick]).cuda()
+    tf = torch.from_numpy(first[pick].astype(np.uint32).view(np.int32)).cuda()
+    ti = torch.from_numpy(pick.astype(np.uint32).view(np.int32)).cuda()
+    _lib.check(L.par2cuda_file_md5_staged_indexed(d.data_ptr(), pitch, len(pick), tl.data_ptr(), tf.data_ptr(),
+                                                 ti.data_ptr(), S, out.data_ptr(), 32, st), "indexed")
+    got, want = out.cpu().numpy().reshape(nf, 16), ref.cpu().numpy().reshape(nf, 16)
+    for f in range(nf):
+        if f in set(pick.tolist()):
+            assert got[f].tobytes() == want[f].tobytes(), f
+        else:
+            assert (got[f] == 0xAB).all(), f
+    assert L.par2cuda_device_error() == 0

@@ -83,3 +83,22 @@ def test_plan_passes_fits_budget():
         need = sum((j.N + j.R) * L.par2cuda_row_pitch_bytes(w) for j, w in zip(jobs, wins))
         assert need <= budget
         assert all(w % 64 == 0 and w * P_ >= j.S for j, w in zip(jobs, wins))   # every byte is in some pass
+
+
+def test_stream_upload_order_staircase():
+    """The job stream's copy order from host buffers: every (job, size class)
+    once; job 0 whole first; class c of jobs past c before class c+1 of any
+    job past c+1; a job's classes in order."""
+    from parpar_gb300.stream import JobStream
+    for n in range(1, 30):
+        for C in range(1, 5):
+            o = JobStream.upload_order(n, C)
+            assert sorted(o) == [(i, c) for i in range(n) for c in range(C)]
+            assert o[:C] == [(0, c) for c in range(C)]
+            pos = {u: k for k, u in enumerate(o)}
+            for i in range(n):
+                assert [pos[i, c] for c in range(C)] == sorted(pos[i, c] for c in range(C))
+            for c in range(C - 1):
+                for i in range(c + 1, n):
+                    for j in range(c + 2, n):
+                        assert pos[i, c] < pos[j, c + 1]
