@@ -141,19 +141,26 @@ class BatchRunner:
                                                     b.d_rec.data_ptr(), b.pw, b.spec.R, self._n_words(n), 0, st),
                        "muladd_index")
         else:
-            # scratch of its own (made on the first, eager, call; the resident
-            # index bytes stay untouched for the persistent launch)
-            if getattr(b, "d_mscratch", None) is None:
-                sb = autotune.scratch_bytes(method, b.spec.R, b.spec.N, self._n_words(b.W))
-                b.d_mscratch = torch.empty(max(sb, 256), dtype=torch.uint8, device=self.dev)
-            _lib.check(self.L.par2cuda_muladd(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_coeff.data_ptr(), b.d_rec.data_ptr(),
-                                              b.pw, b.spec.R, self._n_words(n), 0, autotune.METHODS[method],
-                                              b.d_mscratch.data_ptr(), b.d_mscratch.numel(), st), "muladd")
+            self._muladd_method(b, p, st, method)
+
+    def _muladd_method(self, b: _JobBufs, p: int, st, method: str):
+        """One job's window with a non-comb method, from its coefficients, in
+        scratch of its own (made on the first, eager, call; the resident index
+        bytes stay untouched for the persistent launch)."""
+        off, n = b.window(p)
+        if getattr(b, "d_mscratch", None) is None:
+            sb = autotune.scratch_bytes(method, b.spec.R, b.spec.N, self._n_words(b.W))
+            b.d_mscratch = torch.empty(max(sb, 256), dtype=torch.uint8, device=self.dev)
+        _lib.check(self.L.par2cuda_muladd(b.d_in.data_ptr(), b.pw, b.spec.N, b.d_coeff.data_ptr(), b.d_rec.data_ptr(),
+                                          b.pw, b.spec.R, self._n_words(n), 0, autotune.METHODS[method],
+                                          b.d_mscratch.data_ptr(), b.d_mscratch.numel(), st), "muladd")
 
     # ------------------------------------------------------------ per-job path
-    def run_per_job(self, verify_cb=None):
+    def run_per_job(self, verify_cb=None, tuned_methods: bool = False):
         """Each job on its own: its launches for every pass, then wait for it.
-        Returns per-job wall latencies (s)."""
+        tuned_methods: each job's multiply method is the one the batched path
+        uses for its recovery count (method_of), else the single-job default
+        (comb).  Returns per-job wall latencies (s)."""
         L = self.L
         cur = torch.cuda.current_stream(self.dev)
         st = cur.cuda_stream
@@ -165,7 +172,11 @@ class BatchRunner:
             for p in range(self.P):
                 if not self._window_prep(b, p, st):
                     continue
-                self._muladd_grid(b, p, st)
+                method = self.method_of(b.spec.R) if tuned_methods else "comb"
+                if method == "comb":
+                    self._muladd_grid(b, p, st)
+                else:
+                    self._muladd_method(b, p, st, method)
                 self._verify(b, p, st)
                 if verify_cb:
                     verify_cb(b, p)
