@@ -604,7 +604,7 @@ def plugin_measure(args, cfg, file_lens, local, steps):
     host_in.copy_(tmp)
     del tmp
     rec_host = torch.empty((R, S), dtype=torch.uint8, pin_memory=True)
-    g = GfProc(S, method=args.method, device=local)
+    g = GfProc(S, method=args.plugin_method, device=local, input_batchsize=args.plugin_batch)
     g.set_recovery_slices(list(range(R)))
     L = _lib.load()
     ctx = g._ctx
@@ -1101,6 +1101,10 @@ def main():
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-plugin", action="store_true", help="skip the plugin-boundary e2e measurement")
     ap.add_argument("--plugin-steps", type=int, default=9)
+    ap.add_argument("--plugin-method", choices=["auto", "comb", "xor", "nibble", "tensor", "tensor_fp4"],
+                    default="tensor_fp4", help="backend method of the plugin-boundary measurement")
+    ap.add_argument("--plugin-batch", type=int, default=0,
+                    help="inputs per staging area of the plugin-boundary measurement (0 = the backend's default)")
     ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor", "tensor_fp4"], default="comb",
                     help="multiply-accumulate kernel of the resident-job workloads")
     ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")

@@ -25,10 +25,15 @@ namespace p2c {
 
 const uint16_t* host_input_logs();
 
-static size_t default_batch(size_t slice) {
-	// about 512 MiB of staged input per area, 8..512 inputs, multiple of 8
-	size_t b = (512ull << 20) / (slice ? slice : 1);
-	if(b > 512) b = 512;
+static size_t default_batch(size_t slice, int method) {
+	// about 512 MiB of staged input per area, 8..512 inputs, multiple of 8;
+	// the 4-bit tensor method wants long K (16 bits per input) per GEMM: its
+	// per-tile set-up and epilogue are amortised over more MMAs, so 4 GiB per
+	// area, up to 4096 inputs (2000 x 2 MiB slices: 65 ms per pass through the
+	// plugin calls against 96 ms with 256-input batches)
+	const bool tensor4 = method == 5;
+	size_t b = ((tensor4 ? 4096ull : 512ull) << 20) / (slice ? slice : 1);
+	b = std::min<size_t>(b, tensor4 ? 4096 : 512);
 	if(b < 8) b = 8;
 	return round_up(b, 8);
 }
@@ -187,7 +192,7 @@ int Engine::init(int m, unsigned inputBatch) {
 	if(!sliceSize) { set_error("setSliceSize must be called before init"); return -1; }
 	method = m == 0 ? 1 : m;
 	if(method < 1 || method > 5) { set_error("unknown method %d", m); return -1; }
-	inputBatchSize = inputBatch ? inputBatch : (unsigned)default_batch(sliceSize);
+	inputBatchSize = inputBatch ? inputBatch : (unsigned)default_batch(sliceSize, method);
 	if(inputBatchSize > 32768) { set_error("input batch size %u > 32768", inputBatchSize); return -1; }
 	batchPad = (unsigned)round_up(inputBatchSize, 8);
 	minInBatchSize = inputBatchSize;
