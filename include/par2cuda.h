@@ -332,6 +332,11 @@ int par2cuda_coeff_index(const uint16_t* d_coeff, unsigned num_rec, unsigned num
  * (set_coeffs, gf16/controller_cpu.cpp:372-379, without a host matrix). */
 int par2cuda_par2_index(const uint16_t* d_input_nums, unsigned num_in, const uint16_t* d_exponents, unsigned num_rec,
                         void* d_index, void* stream);
+/* The PAR2 coefficient matrix d_coeff[num_rec][num_in] itself, computed on
+ * the device the same way (gfmat_coeff, gf16/gfmat_coeff.c:60-77), for the
+ * multiply methods of par2cuda_muladd that read coefficients. */
+int par2cuda_par2_coeffs(const uint16_t* d_input_nums, unsigned num_in, const uint16_t* d_exponents, unsigned num_rec,
+                         uint16_t* d_coeff, void* stream);
 /* Work units of a job with num_rec rows of n_words words for batched CTA
  * shape 1..7 (1..4: one-phase, 8 x {1,4,8,12} recovery rows per unit; 5..7:
  * paired tables, {72,64,32} rows per unit); 0 for an unknown shape. */

@@ -105,6 +105,7 @@ SIGNATURES = [
     ("par2cuda_coeff_index_bytes", _sz, [_u, _u]),
     ("par2cuda_coeff_index", _i, [_vp, _u, _u, _vp, _vp]),
     ("par2cuda_par2_index", _i, [_vp, _u, _vp, _u, _vp, _vp]),
+    ("par2cuda_par2_coeffs", _i, [_vp, _u, _vp, _u, _vp, _vp]),
     ("par2cuda_batch_units", ctypes.c_ulonglong, [_u, _sz, _i]),
     ("par2cuda_batch_muladd", _i, [_vp, _u, ctypes.c_ulonglong, _vp, _i, _vp]),
     ("par2cuda_muladd_index", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _vp]),

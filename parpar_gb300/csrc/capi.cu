@@ -281,6 +281,15 @@ int par2cuda_par2_index(const uint16_t* d_input_nums, unsigned num_in, const uin
 	return p2c::par2_idx(d_input_nums, d_exponents, num_rec, num_in, reinterpret_cast<uint4*>(d_index), gt, (cudaStream_t)stream);
 }
 
+int par2cuda_par2_coeffs(const uint16_t* d_input_nums, unsigned num_in, const uint16_t* d_exponents, unsigned num_rec,
+                         uint16_t* d_coeff, void* stream) {
+	int dev = 0;
+	P2C_CUDA_TRY(cudaGetDevice(&dev));
+	p2c::GfTables gt;
+	if(p2c::gf_tables(dev, &gt)) return -1;
+	return p2c::par2_coeffs(d_input_nums, d_exponents, num_rec, num_in, d_coeff, gt, (cudaStream_t)stream);
+}
+
 unsigned long long par2cuda_batch_units(unsigned num_rec, size_t n_words, int shape) {
 	return p2c::comb_units(num_rec, n_words, shape);
 }

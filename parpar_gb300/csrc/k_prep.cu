@@ -196,6 +196,27 @@ int par2_idx(const uint16_t* dNums, const uint16_t* dExp, unsigned R, unsigned n
 	return 0;
 }
 
+// the PAR2 coefficient matrix [R][nIn] itself, from input numbers and
+// exponents (for the methods that read coefficients rather than index bytes)
+__global__ void k_par2_coeffs(const uint16_t* nums, const uint16_t* outExp, unsigned R, unsigned nIn, uint16_t* coeff,
+                              GfTables gt)
+{
+	const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if(id >= (size_t)R * nIn) return;
+	const unsigned r = (unsigned)(id / nIn), i = (unsigned)(id % nIn);
+	coeff[id] = gt.exp[((uint32_t)gt.inLog[nums[i] & 32767] * outExp[r]) % 65535u];
+}
+
+int par2_coeffs(const uint16_t* dNums, const uint16_t* dExp, unsigned R, unsigned nIn, uint16_t* dCoeff,
+                const GfTables& gt, cudaStream_t st)
+{
+	const size_t n = (size_t)R * nIn;
+	if(!n) return 0;
+	k_par2_coeffs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dNums, dExp, R, nIn, dCoeff, gt);
+	P2C_CUDA_TRY(cudaGetLastError());
+	return 0;
+}
+
 // coefficient matrix [R][nIn] -> index layout (used by the device-level entry point)
 __global__ void k_coeff_to_idx(const uint16_t* coeff, unsigned R, unsigned nIn, unsigned G, uint4* idx)
 {

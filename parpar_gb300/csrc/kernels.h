@@ -24,6 +24,8 @@ int coeff_to_idx(const uint16_t* dCoeff, unsigned R, unsigned nIn, uint4* dIdx, 
 // index bytes of PAR2 coefficients from input numbers dNums[nIn] and exponents dExp[R]
 int par2_idx(const uint16_t* dNums, const uint16_t* dExp, unsigned R, unsigned nIn, uint4* dIdx, const GfTables& gt,
              cudaStream_t st);
+int par2_coeffs(const uint16_t* dNums, const uint16_t* dExp, unsigned R, unsigned nIn, uint16_t* dCoeff,
+                const GfTables& gt, cudaStream_t st);
 inline size_t idx_bytes(unsigned R, unsigned nIn) { return (size_t)R * ((nIn + 7) / 8) * 16; }
 
 // rec[r][0..nWords) (^)= sum_i c(r,i) in[i][0..nWords), the comb kernel

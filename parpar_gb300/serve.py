@@ -11,9 +11,13 @@ byte-window passes (PAR2Chunked's chunking, lib/par2.js:837-879) with its
 coefficient index table resident across the passes.  Latency = completion -
 arrival; the loop reports jobs/s and p50/p99 latency.
 
-Per job and window: synthetic slice window, zero pad + checksum, the comb
-multiply-accumulate (one persistent launch over the job's units with the
-resident index table), checksum verification.  All device work goes through
+Per job and window: synthetic slice window, zero pad + checksum, the
+multiply-accumulate, checksum verification.  The multiply method is the
+autotuner's choice for the job's recovery count (autotune.best_method): the
+comb kernel from the job's resident index table (a grid launch, or one
+persistent launch over the job's units), or another method (on GB300 the
+block-scaled 4-bit tensor form) from the job's coefficient matrix, computed
+once on the device, with scratch of its own.  All device work goes through
 libpar2cuda.so's C ABI.
 """
 from __future__ import annotations
@@ -65,18 +69,44 @@ class Server:
         self.launches = 0
 
     # ---------------------------------------------------------------- sizing
+    def _method(self, spec: JobSpec) -> str:
+        return "comb" if self.persistent else autotune.best_method(spec.R)
+
+    @staticmethod
+    def _n_words(W: int) -> int:
+        return ((W + 7) // 8 * 8 + 8) // 2
+
+    def _scratch_bytes(self, spec: JobSpec, method: str, W: int) -> int:
+        """Scratch of a non-comb method for a window of W bytes (0 for comb):
+        the 4-bit tensor method's expanded operands for the whole window, or
+        the index scratch of the others."""
+        if method == "comb":
+            return 0
+        if method == "tensor_fp4":
+            return self.L.par2cuda_tensor_fp4_scratch_bytes(spec.R, spec.N, self._n_words(W))
+        return autotune.scratch_bytes(method, spec.R, spec.N, self._n_words(W))
+
+    def _window_bytes(self, spec: JobSpec, W: int, method: str) -> int:
+        """Device bytes of a window: input and recovery rows, and for a
+        non-comb method its coefficient matrix and scratch."""
+        b = (spec.N + spec.R) * self.L.par2cuda_row_pitch_bytes(W)
+        if method != "comb":
+            b += 2 * spec.R * spec.N + self._scratch_bytes(spec, method, W)
+        return b
+
     def _window(self, spec: JobSpec):
-        """Window bytes so the job's rows fit its share of the budget."""
+        """Window bytes so the job's window fits its share of the budget."""
         share = int(self.budget * self.chunk_share)
+        method = self._method(spec)
         W = spec.S
-        while (spec.N + spec.R) * self.L.par2cuda_row_pitch_bytes(W) > share and W > 64:
+        while self._window_bytes(spec, W, method) > share and W > 64:
             W = max(64, -(-(W // 2) // 64) * 64)
         return W
 
     def footprint(self, spec: JobSpec) -> int:
         W = self._window(spec)
-        pitch = self.L.par2cuda_row_pitch_bytes(W)
-        return (spec.N + spec.R) * pitch + self.L.par2cuda_coeff_index_bytes(spec.R, spec.N) + 4 * (spec.N + spec.R) + 4096
+        return (self._window_bytes(spec, W, self._method(spec)) + self.L.par2cuda_coeff_index_bytes(spec.R, spec.N) +
+                4 * (spec.N + spec.R) + 4096)
 
     # ---------------------------------------------------------------- issue
     def _issue(self, req: Request, si: int):
@@ -99,7 +129,17 @@ class Server:
             d_ok = torch.ones(1, dtype=torch.uint8, device=self.dev)
             counter = torch.zeros(1, dtype=torch.int64, device=self.dev)
         shape = autotune.best_shape(spec.R) if self.persistent else 0
-        _lib.check(L.par2cuda_par2_index(d_nums.data_ptr(), spec.N, d_exps.data_ptr(), spec.R, d_idx.data_ptr(), st), "index")
+        method = self._method(spec)
+        if method == "comb":
+            _lib.check(L.par2cuda_par2_index(d_nums.data_ptr(), spec.N, d_exps.data_ptr(), spec.R, d_idx.data_ptr(), st),
+                       "index")
+            d_coeff = d_scr = None
+        else:
+            with torch.cuda.stream(st_obj):
+                d_coeff = torch.empty((spec.R, spec.N), dtype=torch.int16, device=self.dev)
+                d_scr = torch.empty(max(self._scratch_bytes(spec, method, W), 256), dtype=torch.uint8, device=self.dev)
+            _lib.check(L.par2cuda_par2_coeffs(d_nums.data_ptr(), spec.N, d_exps.data_ptr(), spec.R, d_coeff.data_ptr(), st),
+                       "coeffs")
         n_pass = math.ceil(spec.S / W)
         descs = []
         host_out = []
@@ -115,11 +155,15 @@ class Server:
                 dd = torch.frombuffer(bytearray(jd), dtype=torch.uint8).to(self.dev)
                 descs.append(dd)
                 _lib.check(L.par2cuda_batch_muladd(dd.data_ptr(), 1, units, counter.data_ptr(), shape, st), "muladd")
-            else:
+            elif method == "comb":
                 # grid launch from the resident index bytes (measured faster than
                 # the persistent launch on GB300)
                 _lib.check(L.par2cuda_muladd_index(d_in.data_ptr(), pw, spec.N, d_idx.data_ptr(), d_rec.data_ptr(), pw,
                                                    spec.R, nw, 0, st), "muladd")
+            else:
+                _lib.check(L.par2cuda_muladd(d_in.data_ptr(), pw, spec.N, d_coeff.data_ptr(), d_rec.data_ptr(), pw,
+                                             spec.R, nw, 0, autotune.METHODS[method], d_scr.data_ptr(), d_scr.numel(), st),
+                           "muladd")
             _lib.check(L.par2cuda_rows_checksum(d_rec.data_ptr(), pw, spec.R, None, n, 1, d_flags.data_ptr(),
                                                d_ck.data_ptr(), st), "verify")
             with torch.cuda.stream(st_obj):
@@ -129,7 +173,8 @@ class Server:
             self.launches += 7
         ev = torch.cuda.Event()
         ev.record(st_obj)
-        req.state = dict(tensors=(d_in, d_rec, d_nums, d_exps, d_idx, d_ck, d_flags, counter, descs), ok=d_ok, ev=ev,
+        req.state = dict(tensors=(d_in, d_rec, d_nums, d_exps, d_idx, d_ck, d_flags, counter, descs, d_coeff, d_scr),
+                         ok=d_ok, ev=ev, method=method,
                          host_out=host_out, stream=si)
 
     def _finish(self, req: Request):

@@ -424,3 +424,20 @@ def test_max_input_count():
     out, valid = create_recovery(x, np.full(n, S), np.arange(n), exps, input_batchsize=4096)
     assert valid.all()
     assert np.array_equal(out, O.recover(x, np.full(n, S), np.arange(n), exps))
+
+
+def test_device_par2_coefficient_matrix():
+    """par2cuda_par2_coeffs = the oracle's PAR2 coefficients, including the
+    largest input number and exponent."""
+    import torch
+    L = _lib.load()
+    nums = np.array([0, 1, 2, 3, 100, 4095, 32767], dtype=np.uint16)
+    exps = np.array([0, 1, 2, 300, 12345, 65534], dtype=np.uint16)
+    d_nums = torch.from_numpy(nums.view(np.int16)).cuda()
+    d_exps = torch.from_numpy(exps.view(np.int16)).cuda()
+    out = torch.zeros((len(exps), len(nums)), dtype=torch.int16, device="cuda")
+    _lib.check(L.par2cuda_par2_coeffs(d_nums.data_ptr(), len(nums), d_exps.data_ptr(), len(exps), out.data_ptr(), None),
+               "coeffs")
+    got = out.cpu().numpy().view(np.uint16)
+    want = np.array([[O.coeff(int(i), int(e)) for i in nums] for e in exps], dtype=np.uint16)
+    assert np.array_equal(got, want)
