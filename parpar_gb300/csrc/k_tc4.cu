@@ -22,8 +22,9 @@
 // TMEM columns 0-255, the scale factors (all 1.0) in columns 256-511.  The
 // epilogue reads the accumulators with tcgen05.ld: each thread owns one word
 // and 256 columns, i.e. 16 recovery words, whose bits are the accumulators'
-// parities.  CTAs run in groups of T4_GM word tiles that walk the recovery
-// tiles together, so a group's operand rows are read from HBM about once.
+// parities.  CTAs run in groups of word tiles (as many as keep their A tiles
+// in about 48 MiB of L2) that walk the recovery tiles together, so A is read
+// from HBM once and each B tile once per group.
 // Every wait is bounded (error flag g_tc4_error, no hang).
 #include "common.cuh"
 #include "kernels.h"
@@ -39,7 +40,6 @@ namespace p2c {
 #define T4_STAGE_A (T4_BM * T4_KB)
 #define T4_STAGE_B (T4_BN * T4_KB)
 #define T4_STAGE (T4_STAGE_A + T4_STAGE_B)
-#define T4_GM 8
 #define T4_WAIT (1u << 24)
 #define T4_A_CHUNK_BYTES (1ull << 30)
 
@@ -142,7 +142,7 @@ __device__ __forceinline__ uint32_t t4_idesc() {
 __global__ void __launch_bounds__(128, 1) k_tc4_gemm(const __grid_constant__ CUtensorMap tmA,
                                                    const __grid_constant__ CUtensorMap tmB,
                                                    uint16_t* __restrict__ rec, size_t recPitch, unsigned R,
-                                                   unsigned kBlocks, unsigned mTiles, unsigned nTiles,
+                                                   unsigned kBlocks, unsigned mTiles, unsigned nTiles, unsigned groupM,
                                                    size_t w0, size_t nWords, int accumulate)
 {
 	extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -155,12 +155,12 @@ __global__ void __launch_bounds__(128, 1) k_tc4_gemm(const __grid_constant__ CUt
 	const uint32_t doneBar = barBase + 8u * (2 * T4_NST);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-	// raster: groups of T4_GM word tiles walk the recovery tiles together
+	// raster: groups of groupM word tiles walk the recovery tiles together
 	const unsigned t = blockIdx.x;
-	const unsigned grp = t / (T4_GM * nTiles);
-	const unsigned gm = min((unsigned)T4_GM, mTiles - grp * T4_GM);
-	const unsigned within = t - grp * T4_GM * nTiles;
-	const unsigned mt = grp * T4_GM + within % gm, nt = within / gm;
+	const unsigned grp = t / (groupM * nTiles);
+	const unsigned gm = min(groupM, mTiles - grp * groupM);
+	const unsigned within = t - grp * groupM * nTiles;
+	const unsigned mt = grp * groupM + within % gm, nt = within / gm;
 
 	if(threadIdx.x == 0) {
 		for(int s = 0; s < T4_NST; s++) {
@@ -254,11 +254,14 @@ __global__ void __launch_bounds__(128, 1) k_tc4_gemm(const __grid_constant__ CUt
 			               "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
 			             : "r"(tmem + lane0 + 32 * q));
 			asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+			// parity of an exact integer n < 2^23 held in fp32: n + 2^23 has
+			// unit ulp, so bit 0 of its encoding is bit 0 of n (one full-rate
+			// add instead of a float-to-integer conversion per column)
 			uint32_t word0 = 0, word1 = 0;
 #pragma unroll
 			for(int c = 0; c < 16; c++) {
-				word0 |= (__float2uint_rz(__uint_as_float(v[c])) & 1u) << c;
-				word1 |= (__float2uint_rz(__uint_as_float(v[16 + c])) & 1u) << c;
+				word0 |= (__float_as_uint(__fadd_rn(__uint_as_float(v[c]), 8388608.0f)) & 1u) << c;
+				word1 |= (__float_as_uint(__fadd_rn(__uint_as_float(v[16 + c]), 8388608.0f)) & 1u) << c;
 			}
 			const unsigned r0 = nt * 16 + 2 * q;
 			if(w < nWords) {
@@ -327,6 +330,12 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 		if(!accumulate) P2C_CUDA_TRY(cudaMemset2DAsync(rec, recPitch * 2, 0, nWords * 2, R, st));
 		return 0;
 	}
+	if(nIn >= (1u << 19)) {
+		// a column sums up to 16 x nIn ones; the epilogue's parity read needs
+		// the sum below 2^23
+		set_error("tensor method (mxf4): %u inputs in one call, at most %u", nIn, (1u << 19) - 1);
+		return -1;
+	}
 	const size_t kBytes = t4_kbytes(nIn);
 	const unsigned nInPad = (unsigned)(kBytes / 8), rPad = (unsigned)round_up(R, 16);
 	const size_t bBytes = round_up(t4_bbytes(R, nIn), 1024);
@@ -349,6 +358,10 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 	P2C_CUDA_TRY(cudaFuncSetAttribute(k_tc4_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const unsigned nTiles = rPad / 16;
 	const unsigned kBlocks = (unsigned)(kBytes / T4_KB);
+	// word tiles per raster group: their A tiles (128 x kBytes each) stay in
+	// L2 (about 48 MiB of it) while the group walks the recovery tiles, so A
+	// is read from HBM once and each B tile once per group
+	const unsigned groupM = (unsigned)std::min<size_t>(64, std::max<size_t>(8, (48ull << 20) / ((size_t)T4_BM * kBytes)));
 	for(size_t w0 = 0; w0 < nWords; w0 += wChunk) {
 		const size_t rows = std::min(wChunk, round_up(nWords - w0, T4_BM));
 		dim3 pg((unsigned)(rows / 64), (nInPad + 63) / 64);
@@ -357,7 +370,7 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 		CUtensorMap tmA;
 		if(t4_map(&tmA, A, kBytes, rows, T4_BM)) return -1;
 		const unsigned mTiles = (unsigned)(rows / T4_BM);
-		k_tc4_gemm<<<mTiles * nTiles, 128, smem, st>>>(tmA, tmB, rec, recPitch, R, kBlocks, mTiles, nTiles, w0, nWords,
+		k_tc4_gemm<<<mTiles * nTiles, 128, smem, st>>>(tmA, tmB, rec, recPitch, R, kBlocks, mTiles, nTiles, groupM, w0, nWords,
 		                                               accumulate);
 		P2C_CUDA_TRY(cudaGetLastError());
 	}
