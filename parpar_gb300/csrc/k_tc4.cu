@@ -14,17 +14,19 @@
 // word chunk of the inputs at a time), the coefficient matrix to its bit rows
 // (k_tc4_prep_coeff).
 //
-// GEMM CTA (128 threads): one 128-word x 256-bit-row tile (16 recovery
-// slices), all K.  Thread 0 issues the TMA loads of a 4-stage ring (A: 128
-// rows x 128 bytes, B: 256 rows x 128 bytes, 128-byte swizzle) completing on
-// "full" mbarriers; thread 32 issues 4 MMAs (M=128, N=256, K=64) per stage and
-// commits each stage to its "empty" mbarrier; the fp32 accumulators live in
-// TMEM columns 0-255, the scale factors (all 1.0) in columns 256-511.  The
-// epilogue reads the accumulators with tcgen05.ld: each thread owns one word
-// and 256 columns, i.e. 16 recovery words, whose bits are the accumulators'
-// parities.  CTAs run in groups of word tiles (as many as keep their A tiles
-// in about 48 MiB of L2) that walk the recovery tiles together, so A is read
-// from HBM once and each B tile once per group.
+// GEMM: persistent, one CTA of 192 threads per SM walking 128-word x
+// 256-bit-row tiles (16 recovery slices, all K) in raster order.  Thread 0
+// issues the TMA loads of a 4-stage ring (A: 128 rows x 128 bytes, B: 256
+// rows x 128 bytes, 128-byte swizzle) completing on "full" mbarriers, across
+// tile boundaries; thread 32 issues 4 MMAs (M=128, N=256, K=64) per stage and
+// commits each stage to its "empty" mbarrier and each tile to "tmemFull"; the
+// fp32 accumulators live in TMEM columns 0-255, the scale factors (all 1.0)
+// in columns 256-511.  Warps 2-5 read the accumulators with tcgen05.ld (each
+// thread one word and 256 columns, i.e. 16 recovery words, whose bits are the
+// accumulators' parities) and release them through "tmemEmpty" before the
+// next tile's MMAs.  Tiles are grouped by word tiles (as many as keep their A
+// tiles in about 48 MiB of L2) that walk the recovery tiles together, so A is
+// read from HBM once and each B tile once per group.
 // Every wait is bounded (error flag g_tc4_error, no hang).
 #include "common.cuh"
 #include "kernels.h"
@@ -41,6 +43,7 @@ namespace p2c {
 #define T4_STAGE_B (T4_BN * T4_KB)
 #define T4_STAGE (T4_STAGE_A + T4_STAGE_B)
 #define T4_WAIT (1u << 24)
+#define T4_THREADS 192
 #define T4_A_CHUNK_BYTES (1ull << 30)
 
 __device__ unsigned g_tc4_error;
@@ -139,40 +142,74 @@ __device__ __forceinline__ uint32_t t4_idesc() {
 	return (1u << 7) | (1u << 10) | ((uint32_t)(T4_BN >> 3) << 17) | (1u << 23) | ((uint32_t)(T4_BM >> 4) << 24);
 }
 
-__global__ void __launch_bounds__(128, 1) k_tc4_gemm(const __grid_constant__ CUtensorMap tmA,
-                                                   const __grid_constant__ CUtensorMap tmB,
-                                                   uint16_t* __restrict__ rec, size_t recPitch, unsigned R,
-                                                   unsigned kBlocks, unsigned mTiles, unsigned nTiles, unsigned groupM,
-                                                   size_t w0, size_t nWords, int accumulate)
+// tile t -> (word tile mt, recovery tile nt): groups of groupM word tiles walk
+// the recovery tiles together
+__device__ __forceinline__ void t4_tile(unsigned t, unsigned mTiles, unsigned nTiles, unsigned groupM, unsigned& mt,
+                                        unsigned& nt) {
+	const unsigned grp = t / (groupM * nTiles);
+	const unsigned gm = min(groupM, mTiles - grp * groupM);
+	const unsigned within = t - grp * groupM * nTiles;
+	mt = grp * groupM + within % gm;
+	nt = within / gm;
+}
+
+// bounded wait that also gives up when another role of the CTA has given up
+// (flag in shared memory), so that one failed wait ends the whole CTA quickly
+__device__ __forceinline__ bool t4_wait_ab(uint32_t bar, uint32_t parity, volatile uint32_t* abortFlag) {
+	for(unsigned i = 0; i < T4_WAIT; i++) {
+		uint32_t ok;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+		if(ok) return true;
+		if((i & 1023u) == 1023u && *abortFlag) return false;
+	}
+	atomicExch(&g_tc4_error, 1u);
+	*abortFlag = 1u;
+	return false;
+}
+
+// Persistent GEMM: one CTA per SM walks the tiles blockIdx.x, blockIdx.x +
+// gridDim.x, ... in raster order.  Warp 0 (one thread) streams both
+// operands' k-blocks of its tiles through the ring without stopping at tile
+// boundaries; warp 1 (one thread) issues the MMAs, and before the first MMA of
+// a tile waits until the epilogue has read the previous tile's accumulators
+// out of TMEM; warps 2-5 (each the TMEM lane quarter warp % 4) are the
+// epilogue.  So the ring refills while a tile's results are written, and the
+// per-CTA set-up (barriers, TMEM allocation, scale factors) is paid once per
+// SM instead of once per tile.
+__global__ void __launch_bounds__(T4_THREADS, 1) k_tc4_gemm(const __grid_constant__ CUtensorMap tmA,
+                                                          const __grid_constant__ CUtensorMap tmB,
+                                                          uint16_t* __restrict__ rec, size_t recPitch, unsigned R,
+                                                          unsigned kBlocks, unsigned mTiles, unsigned nTiles,
+                                                          unsigned groupM, size_t w0, size_t nWords, int accumulate)
 {
 	extern __shared__ __align__(1024) uint8_t smem_raw[];
 	const uint32_t raw = t4_saddr(smem_raw);
 	const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
 	uint8_t* sm = smem_raw + pad;
 	const uint32_t sbase = raw + pad;
-	const uint32_t barBase = sbase + T4_NST * T4_STAGE;        // full[NST], empty[NST], done
-	uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + T4_NST * T4_STAGE + (2 * T4_NST + 1) * 8);
-	const uint32_t doneBar = barBase + 8u * (2 * T4_NST);
+	// full[NST], empty[NST], tmemFull, tmemEmpty, drain
+	const uint32_t barBase = sbase + T4_NST * T4_STAGE;
+	const uint32_t tmemFull = barBase + 8u * (2 * T4_NST), tmemEmpty = tmemFull + 8u, drainBar = tmemFull + 16u;
+	uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + T4_NST * T4_STAGE + (2 * T4_NST + 3) * 8);
+	volatile uint32_t* abortFlag = tslot + 1;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-	// raster: groups of groupM word tiles walk the recovery tiles together
-	const unsigned t = blockIdx.x;
-	const unsigned grp = t / (groupM * nTiles);
-	const unsigned gm = min(groupM, mTiles - grp * groupM);
-	const unsigned within = t - grp * groupM * nTiles;
-	const unsigned mt = grp * groupM + within % gm, nt = within / gm;
+	const unsigned nAll = mTiles * nTiles;
 
 	if(threadIdx.x == 0) {
 		for(int s = 0; s < T4_NST; s++) {
 			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barBase + 8u * s) : "memory");
 			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barBase + 8u * (T4_NST + s)) : "memory");
 		}
-		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(doneBar) : "memory");
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(tmemFull) : "memory");
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" :: "r"(tmemEmpty) : "memory");
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(drainBar) : "memory");
+		*abortFlag = 0u;
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		asm volatile("prefetch.tensormap [%0];" :: "l"(&tmA) : "memory");
 		asm volatile("prefetch.tensormap [%0];" :: "l"(&tmB) : "memory");
 	}
-	if(warp == 0) {
+	if(warp == 1) {
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(t4_saddr(tslot)), "r"(512u) : "memory");
 		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 	}
@@ -181,10 +218,11 @@ __global__ void __launch_bounds__(128, 1) k_tc4_gemm(const __grid_constant__ CUt
 	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 	const uint32_t tmem = *tslot;
 
-	// scale factors: TMEM columns 256-511 of every lane hold ue8m0 1.0 bytes
-	{
+	// scale factors: TMEM columns 256-511 of every lane hold ue8m0 1.0 bytes;
+	// each epilogue warp fills its own lane quarter
+	if(warp >= 2) {
 		const uint32_t one = 0x7F7F7F7Fu;
-		const uint32_t lane0 = (uint32_t)(32 * warp) << 16;
+		const uint32_t lane0 = (uint32_t)(32 * (warp & 3)) << 16;
 #pragma unroll
 		for(int q = 0; q < 8; q++)
 			asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
@@ -196,89 +234,130 @@ __global__ void __launch_bounds__(128, 1) k_tc4_gemm(const __grid_constant__ CUt
 	__syncthreads();
 	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-	if(threadIdx.x == 0) {
-		// TMA producer
-		for(unsigned kb = 0; kb < kBlocks; kb++) {
-			const unsigned s = kb % T4_NST;
-			if(kb >= T4_NST && !t4_wait(barBase + 8u * (T4_NST + s), ((kb / T4_NST) - 1) & 1)) break;
-			const uint32_t full = barBase + 8u * s;
-			const uint32_t dA = sbase + s * T4_STAGE, dB = dA + T4_STAGE_A;
-			asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
-			             :: "r"(full), "r"((uint32_t)T4_STAGE) : "memory");
-			const int x = (int)(kb * T4_KB);
-			asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-			             :: "r"(dA), "l"(&tmA), "r"(x), "r"((int)(mt * T4_BM)), "r"(full) : "memory");
-			asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-			             :: "r"(dB), "l"(&tmB), "r"(x), "r"((int)(nt * T4_BN)), "r"(full) : "memory");
-		}
-	} else if(threadIdx.x == 32) {
-		// MMA issuer
-		const uint32_t idesc = t4_idesc();
-		const uint32_t sfa = tmem + 256, sfb = tmem + 384;
-		for(unsigned kb = 0; kb < kBlocks; kb++) {
-			const unsigned s = kb % T4_NST;
-			if(!t4_wait(barBase + 8u * s, (kb / T4_NST) & 1)) break;
-			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-			const uint32_t aS = sbase + s * T4_STAGE, bS = aS + T4_STAGE_A;
-#pragma unroll
-			for(int k = 0; k < 4; k++) {
-				const uint64_t ad = t4_desc(aS + k * 32), bd = t4_desc(bS + k * 32);
-				const uint32_t acc = (kb | k) != 0;
-				asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
-				             "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], [%5], p;\n\t}"
-				             :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(sfa), "r"(sfb), "r"(acc) : "memory");
+	if(warp == 0) {
+		if(lane == 0) {
+			// TMA producer: k-block g of the CTA's sequence goes to stage g % NST
+			uint32_t g = 0;
+			bool ok = true;
+			for(unsigned t = blockIdx.x; t < nAll && ok; t += gridDim.x) {
+				unsigned mt, nt;
+				t4_tile(t, mTiles, nTiles, groupM, mt, nt);
+				for(unsigned kb = 0; kb < kBlocks; kb++, g++) {
+					const unsigned s = g % T4_NST;
+					if(g >= T4_NST && !t4_wait_ab(barBase + 8u * (T4_NST + s), ((g / T4_NST) - 1) & 1, abortFlag)) {
+						ok = false;
+						break;
+					}
+					const uint32_t full = barBase + 8u * s;
+					const uint32_t dA = sbase + s * T4_STAGE, dB = dA + T4_STAGE_A;
+					asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+					             :: "r"(full), "r"((uint32_t)T4_STAGE) : "memory");
+					const int x = (int)(kb * T4_KB);
+					asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+					             :: "r"(dA), "l"(&tmA), "r"(x), "r"((int)(mt * T4_BM)), "r"(full) : "memory");
+					asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+					             :: "r"(dB), "l"(&tmB), "r"(x), "r"((int)(nt * T4_BN)), "r"(full) : "memory");
+				}
 			}
-			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-			             :: "r"(barBase + 8u * (T4_NST + s)) : "memory");
+			if(!ok) {
+				// let the copies still in flight land before the CTA ends
+				for(uint32_t h = g > T4_NST ? g - T4_NST : 0; h < g; h++)
+					t4_wait(barBase + 8u * (h % T4_NST), (h / T4_NST) & 1);
+			}
 		}
-		asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(doneBar) : "memory");
+	} else if(warp == 1) {
+		if(lane == 0) {
+			// MMA issuer
+			const uint32_t idesc = t4_idesc();
+			const uint32_t sfa = tmem + 256, sfb = tmem + 384;
+			uint32_t g = 0, i = 0;
+			bool ok = true;
+			for(unsigned t = blockIdx.x; t < nAll && ok; t += gridDim.x, i++) {
+				// the epilogue has read the previous tile's accumulators
+				if(i > 0 && !t4_wait_ab(tmemEmpty, (i - 1) & 1, abortFlag)) { ok = false; break; }
+				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				for(unsigned kb = 0; kb < kBlocks; kb++, g++) {
+					const unsigned s = g % T4_NST;
+					if(!t4_wait_ab(barBase + 8u * s, (g / T4_NST) & 1, abortFlag)) { ok = false; break; }
+					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+					const uint32_t aS = sbase + s * T4_STAGE, bS = aS + T4_STAGE_A;
+#pragma unroll
+					for(int k = 0; k < 4; k++) {
+						const uint64_t ad = t4_desc(aS + k * 32), bd = t4_desc(bS + k * 32);
+						const uint32_t acc = (kb | k) != 0;
+						asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
+						             "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], [%5], p;\n\t}"
+						             :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(sfa), "r"(sfb), "r"(acc) : "memory");
+					}
+					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+					             :: "r"(barBase + 8u * (T4_NST + s)) : "memory");
+				}
+				if(ok)
+					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+					             :: "r"(tmemFull) : "memory");
+			}
+			// every MMA this thread issued has completed before TMEM is freed
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+			             :: "r"(drainBar) : "memory");
+			t4_wait(drainBar, 0);
+		}
+	} else {
+		// epilogue: thread (warp, lane) owns word mt*128 + 32*(warp%4) + lane
+		// and the 256 accumulator columns of its TMEM lane = 16 recovery words
+		const unsigned quarter = warp & 3;
+		const uint32_t lane0 = (uint32_t)(32 * quarter) << 16;
+		uint32_t i = 0;
+		for(unsigned t = blockIdx.x; t < nAll; t += gridDim.x, i++) {
+			unsigned mt, nt;
+			t4_tile(t, mTiles, nTiles, groupM, mt, nt);
+			const bool ok = __all_sync(0xffffffffu, t4_wait_ab(tmemFull, i & 1, abortFlag));
+			if(!ok) break;
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+			const size_t w = w0 + (size_t)mt * T4_BM + 32 * quarter + lane;
+#pragma unroll 1
+			for(int q = 0; q < 8; q++) {
+				uint32_t v[32];
+				asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+				             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+				             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+				             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+				               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+				               "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+				               "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+				             : "r"(tmem + lane0 + 32 * q));
+				asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+				// parity of an exact integer n < 2^23 held in fp32: n + 2^23 has
+				// unit ulp, so bit 0 of its encoding is bit 0 of n (one full-rate
+				// add instead of a float-to-integer conversion per column)
+				uint32_t word0 = 0, word1 = 0;
+#pragma unroll
+				for(int c = 0; c < 16; c++) {
+					word0 |= (__float_as_uint(__fadd_rn(__uint_as_float(v[c]), 8388608.0f)) & 1u) << c;
+					word1 |= (__float_as_uint(__fadd_rn(__uint_as_float(v[16 + c]), 8388608.0f)) & 1u) << c;
+				}
+				const unsigned r0 = nt * 16 + 2 * q;
+				if(w < nWords) {
+					if(r0 < R) {
+						uint16_t* p = rec + (size_t)r0 * recPitch + w;
+						*p = accumulate ? (uint16_t)(*p ^ word0) : (uint16_t)word0;
+					}
+					if(r0 + 1 < R) {
+						uint16_t* p = rec + (size_t)(r0 + 1) * recPitch + w;
+						*p = accumulate ? (uint16_t)(*p ^ word1) : (uint16_t)word1;
+					}
+				}
+			}
+			// this warp's TMEM reads are done: the next tile's MMAs may start
+			asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+			__syncwarp();
+			if(lane == 0) asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" :: "r"(tmemEmpty) : "memory");
+		}
 	}
 	__syncwarp();
-
-	// epilogue: thread (warp, lane) owns word mt*128 + 32*warp + lane and the
-	// 256 accumulator columns of its TMEM lane = 16 recovery words
-	const bool ok = t4_wait(doneBar, 0);
-	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-	if(ok) {
-		const size_t w = w0 + (size_t)mt * T4_BM + 32 * warp + lane;
-		const uint32_t lane0 = (uint32_t)(32 * warp) << 16;
-#pragma unroll 1
-		for(int q = 0; q < 8; q++) {
-			uint32_t v[32];
-			asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-			             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-			             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-			             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-			               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-			               "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-			               "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-			             : "r"(tmem + lane0 + 32 * q));
-			asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-			// parity of an exact integer n < 2^23 held in fp32: n + 2^23 has
-			// unit ulp, so bit 0 of its encoding is bit 0 of n (one full-rate
-			// add instead of a float-to-integer conversion per column)
-			uint32_t word0 = 0, word1 = 0;
-#pragma unroll
-			for(int c = 0; c < 16; c++) {
-				word0 |= (__float_as_uint(__fadd_rn(__uint_as_float(v[c]), 8388608.0f)) & 1u) << c;
-				word1 |= (__float_as_uint(__fadd_rn(__uint_as_float(v[16 + c]), 8388608.0f)) & 1u) << c;
-			}
-			const unsigned r0 = nt * 16 + 2 * q;
-			if(w < nWords) {
-				if(r0 < R) {
-					uint16_t* p = rec + (size_t)r0 * recPitch + w;
-					*p = accumulate ? (uint16_t)(*p ^ word0) : (uint16_t)word0;
-				}
-				if(r0 + 1 < R) {
-					uint16_t* p = rec + (size_t)(r0 + 1) * recPitch + w;
-					*p = accumulate ? (uint16_t)(*p ^ word1) : (uint16_t)word1;
-				}
-			}
-		}
-	}
 	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 	__syncthreads();
-	if(warp == 0)
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	if(warp == 1)
 		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(512u) : "memory");
 }
 
@@ -354,8 +433,11 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 	P2C_CUDA_TRY(cudaGetLastError());
 	CUtensorMap tmB;
 	if(t4_map(&tmB, B, kBytes, (size_t)rPad * 16, T4_BN)) return -1;
-	const size_t smem = T4_NST * T4_STAGE + (2 * T4_NST + 1) * 8 + 16 + 1024;
+	const size_t smem = T4_NST * T4_STAGE + (2 * T4_NST + 3) * 8 + 16 + 1024;
 	P2C_CUDA_TRY(cudaFuncSetAttribute(k_tc4_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	int dev = 0, nSM = 0;
+	P2C_CUDA_TRY(cudaGetDevice(&dev));
+	P2C_CUDA_TRY(cudaDeviceGetAttribute(&nSM, cudaDevAttrMultiProcessorCount, dev));
 	const unsigned nTiles = rPad / 16;
 	const unsigned kBlocks = (unsigned)(kBytes / T4_KB);
 	// word tiles per raster group: their A tiles (128 x kBytes each) stay in
@@ -370,7 +452,9 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 		CUtensorMap tmA;
 		if(t4_map(&tmA, A, kBytes, rows, T4_BM)) return -1;
 		const unsigned mTiles = (unsigned)(rows / T4_BM);
-		k_tc4_gemm<<<mTiles * nTiles, 128, smem, st>>>(tmA, tmB, rec, recPitch, R, kBlocks, mTiles, nTiles, groupM, w0, nWords,
+		// one CTA per SM (its shared memory allows no second), each walking tiles
+		const unsigned grid = (unsigned)std::min<size_t>((size_t)mTiles * nTiles, (size_t)std::max(nSM, 1));
+		k_tc4_gemm<<<grid, T4_THREADS, smem, st>>>(tmA, tmB, rec, recPitch, R, kBlocks, mTiles, nTiles, groupM, w0, nWords,
 		                                               accumulate);
 		P2C_CUDA_TRY(cudaGetLastError());
 	}
