@@ -1105,8 +1105,8 @@ def main():
                     default="tensor_fp4", help="backend method of the plugin-boundary measurement")
     ap.add_argument("--plugin-batch", type=int, default=0,
                     help="inputs per staging area of the plugin-boundary measurement (0 = the backend's default)")
-    ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor", "tensor_fp4"], default="comb",
-                    help="multiply-accumulate kernel of the resident-job workloads")
+    ap.add_argument("--method", choices=["auto", "comb", "xor", "nibble", "tensor", "tensor_fp4"], default="tensor_fp4",
+                    help="multiply-accumulate kernel of the resident-job workloads and the job stream")
     ap.add_argument("--budget-gib", type=int, default=64, help="HBM budget of one pass of the batched workload")
     ap.add_argument("--comb-shape", type=int, default=0,
                     help="pin the comb kernel's CTA shape (par2cuda_set_comb_shape; 0 = automatic)")

@@ -173,6 +173,15 @@ uint16_t par2cuda_coeff(uint16_t input_num, uint16_t exponent);
  * builder warpgroup's registers moved to the lookup warps (84, 72 and 96
  * rows).  Returns the previous setting. */
 int par2cuda_set_comb_shape(int shape);
+/* Tile shape of the block-scaled 4-bit tensor method for every later call in
+ * this process (the autotuner's knob): 0 = chosen from the number of inputs,
+ * 1 = 128 words x 16 recovery slices with one TMEM accumulator, 2 = 128 words
+ * x 12 recovery slices with two accumulators (a tile's read-out overlaps the
+ * next tile's MMAs).  Returns the previous setting.  No counterpart in the
+ * reference. */
+int par2cuda_set_tc4_shape(int shape);
+/* The tile shape (1 or 2) the next tensor_fp4 call with num_in inputs will use. */
+int par2cuda_tc4_shape_for(unsigned num_in);
 /* Measures the rate (bytes/s) of one MD5 stream on one GPU thread with its
  * data in registers (about 0.1 s): the dependency-chain ceiling of the
  * one-stream-per-thread hash kernels (file MD5, IFSC, recovery-packet MD5).

@@ -83,9 +83,10 @@ def scratch_bytes(method: str, R: int, N: int, n_words: int) -> int:
     L = _lib.load()
     if method == "tensor_fp4":
         full = L.par2cuda_tensor_fp4_scratch_bytes(R, N, n_words)
-        kbytes = (N + 15) // 16 * 16 * 8
-        bbytes = ((R + 15) // 16 * 16 * 16 * kbytes + 1023) // 1024 * 1024
-        return min(full, bbytes + max(FP4_CHUNK_BYTES, 128 * kbytes))
+        # one 128-word tile of expanded input planes (8 bytes per input, 16-input steps)
+        one_tile = ((N + 15) // 16 * 16 * 8 * 128 + 1023) // 1024 * 1024
+        fixed = L.par2cuda_tensor_fp4_scratch_bytes(R, N, 1) - one_tile   # tile counter + coefficient bit matrix
+        return min(full, fixed + (max(FP4_CHUNK_BYTES, one_tile) + 1023) // 1024 * 1024)
     return L.par2cuda_muladd_scratch_bytes(R, N)
 
 

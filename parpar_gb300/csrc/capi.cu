@@ -130,6 +130,13 @@ int par2cuda_set_comb_shape(int shape) {
 	return p2c::set_comb_shape(shape);
 }
 
+int par2cuda_set_tc4_shape(int shape) {
+	if(shape < 0 || shape > 2) { p2c::set_error("tensor_fp4 tile shape %d out of range 0..2", shape); return -1; }
+	return p2c::set_tc4_shape(shape);
+}
+
+int par2cuda_tc4_shape_for(unsigned num_in) { return p2c::tc4_shape_for((unsigned)((num_in + 15) / 16)); }
+
 int par2cuda_md5_chain_rate(double* bytes_per_s, void* stream) {
 	if(!bytes_per_s) { p2c::set_error("md5_chain_rate: null output"); return -1; }
 	return p2c::md5_chain_rate(bytes_per_s, (cudaStream_t)stream);

@@ -151,10 +151,7 @@ int Engine::alloc_desc() {
 size_t Engine::fp4_scratch_bytes() const {
 	// the coefficient bit matrix of a full batch plus word chunks of at most
 	// 512 MiB of expanded input planes
-	const size_t kBytes = round_up(batchPad, 16) * 8;
-	const size_t bBytes = round_up(round_up(std::max<size_t>(outputExponents.size(), 1), 16) * 16 * kBytes, 1024);
-	return std::min(tc4_scratch_bytes((unsigned)outputExponents.size(), batchPad, row_words(allocSliceSize)),
-	                bBytes + std::max<size_t>(512ull << 20, 128 * kBytes));
+	return tc4_scratch_chunked_bytes((unsigned)outputExponents.size(), batchPad, row_words(allocSliceSize), 512ull << 20);
 }
 
 int Engine::alloc_processing() {

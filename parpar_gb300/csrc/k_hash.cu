@@ -16,7 +16,9 @@
 
 namespace p2c {
 
-__constant__ uint32_t c_md5K[64] = {
+// RFC 1321 round constants (a constexpr table: indexed by the unrolled step
+// number, each becomes an immediate operand).
+__device__ constexpr uint32_t c_md5K[64] = {
 	0xd76aa478,0xe8c7b756,0x242070db,0xc1bdceee,0xf57c0faf,0x4787c62a,0xa8304613,0xfd469501,
 	0x698098d8,0x8b44f7af,0xffff5bb1,0x895cd7be,0x6b901122,0xfd987193,0xa679438e,0x49b40821,
 	0xf61e2562,0xc040b340,0x265e5a51,0xe9b6c7aa,0xd62f105d,0x02441453,0xd8a1e681,0xe7d3fbc8,
@@ -38,7 +40,15 @@ __device__ __forceinline__ void md5_block(uint32_t st[4], const uint32_t m[16]) 
 		else if(i < 32) { f = c ^ (d & (b ^ c)); g = (5 * i + 1) & 15; s = (i & 3) == 0 ? 5 : (i & 3) == 1 ? 9 : (i & 3) == 2 ? 14 : 20; }
 		else if(i < 48) { f = b ^ c ^ d; g = (3 * i + 5) & 15; s = (i & 3) == 0 ? 4 : (i & 3) == 1 ? 11 : (i & 3) == 2 ? 16 : 23; }
 		else { f = c ^ (b | ~d); g = (7 * i) & 15; s = (i & 3) == 0 ? 6 : (i & 3) == 1 ? 10 : (i & 3) == 2 ? 15 : 21; }
-		uint32_t t = a + f + c_md5K[i] + m[g];
+		// a + K + m does not depend on the previous step; the add of f is the
+		// only add on the step's dependency chain (LOP3 -> add -> rotate-add).
+		// It is written as its own PTX add so that the compiler cannot fold f
+		// into the off-chain sum: with the four terms in one C expression the
+		// step compiled to a second dependent add and ran ~21 cycles instead
+		// of ~17 on GB300 with message words loaded from memory.
+		const uint32_t pre = a + c_md5K[i] + m[g];
+		uint32_t t;
+		asm("add.u32 %0, %1, %2;" : "=r"(t) : "r"(f), "r"(pre));
 		a = d; d = c; c = b;
 		b = b + rotl(t, s);
 	}
@@ -257,23 +267,20 @@ int slice_hash(const void* rows, size_t pitchBytes, unsigned n, const uint32_t* 
 
 // ---- calibration: the MD5 dependency-chain bound ------------------------------
 // One MD5 stream on one GPU thread is bound by the latency of its serial
-// step chain (4 dependent integer ops per step), not by memory.  This kernel
-// runs that chain on register-resident data, one warp on one SM: the bytes/s
-// of one lane is the ceiling for the per-file and per-slice hash kernels.  The
-// message words depend on the block counter only, so, as with words loaded
-// ahead from memory, they stay off the chain; the chain itself carries across
-// blocks, so nothing can be hoisted.
+// step chain (3 dependent integer ops per step: the round function, the add
+// of a + K + m, the rotate-and-add), not by memory.  This kernel runs that
+// chain on register-resident data, one warp on one SM: the bytes/s of one
+// lane is the ceiling for the per-file and per-slice hash kernels.  The state
+// carries across blocks, so no block's work can be hoisted.
 __global__ void __launch_bounds__(32) k_md5_chain(uint32_t* sink, unsigned blocks) {
 	uint32_t st[4] = {0x67452301u ^ threadIdx.x, 0xefcdab89u, 0x98badcfeu, 0x10325476u};
-	uint32_t base[16];
+	// the same message block every time, held in registers: each step's
+	// a + K + m term has nothing to wait for, so the loop runs at the step
+	// chain's own latency (LOP3 -> add -> rotate-add)
+	uint32_t m[16];
 #pragma unroll
-	for(int q = 0; q < 16; q++) base[q] = (uint32_t)(q + 1) * 0x9E3779B9u ^ threadIdx.x;
-	for(unsigned b = 0; b < blocks; b++) {
-		uint32_t m[16];
-#pragma unroll
-		for(int q = 0; q < 16; q++) m[q] = base[q] + b;
-		md5_block(st, m);
-	}
+	for(int q = 0; q < 16; q++) m[q] = (uint32_t)(q + 1) * 0x9E3779B9u ^ threadIdx.x;
+	for(unsigned b = 0; b < blocks; b++) md5_block(st, m);
 	if((st[0] ^ st[1] ^ st[2] ^ st[3]) == 0x5EEDF00Du && blocks == 0) sink[threadIdx.x] = st[0];
 }
 

@@ -14,34 +14,65 @@
 // word chunk of the inputs at a time), the coefficient matrix to its bit rows
 // (k_tc4_prep_coeff).
 //
-// GEMM: persistent, one CTA of 192 threads per SM walking 128-word x
-// 256-bit-row tiles (16 recovery slices, all K) in raster order.  Thread 0
-// issues the TMA loads of a 4-stage ring (A: 128 rows x 128 bytes, B: 256
-// rows x 128 bytes, 128-byte swizzle) completing on "full" mbarriers, across
-// tile boundaries; thread 32 issues 4 MMAs (M=128, N=256, K=64) per stage and
-// commits each stage to its "empty" mbarrier and each tile to "tmemFull"; the
-// fp32 accumulators live in TMEM columns 0-255, the scale factors (all 1.0)
-// in columns 256-511.  Warps 2-5 read the accumulators with tcgen05.ld (each
-// thread one word and 256 columns, i.e. 16 recovery words, whose bits are the
-// accumulators' parities) and release them through "tmemEmpty" before the
-// next tile's MMAs.  Tiles are grouped by word tiles (as many as keep their A
-// tiles in about 48 MiB of L2) that walk the recovery tiles together, so A is
-// read from HBM once and each B tile once per group.
+// GEMM: persistent, one CTA of 192 threads per SM taking 128-word x
+// 256-bit-row tiles (16 recovery slices, all K) from a global tile counter,
+// in raster order, so that a CTA that starts late (its SM held by another
+// kernel) simply takes fewer tiles.  Thread 0 issues the TMA loads of a
+// 4-stage ring (A: 128 rows x 128 bytes, B: 256 rows x 128 bytes, 128-byte
+// swizzle) completing on "full" mbarriers, across tile boundaries, and
+// publishes each tile number to the other roles; thread 32 issues 4 MMAs
+// (M=128, N=256, K=64) per stage into the TMEM accumulator (columns 0-255;
+// the scale factors, all 1.0, in columns 448-511) and commits each stage to
+// its "empty" mbarrier and each tile to "tmemFull"; warps 2-5 read the
+// accumulator with tcgen05.ld (each thread one word and 256 columns, i.e. 16
+// recovery words, whose bits are the accumulators' parities) and release it.
+// A second tile shape (192 rows, two accumulators) can be selected.  Tiles
+// are grouped by word tiles (as many as keep their A tiles in about 48 MiB of
+// L2) that walk the recovery tiles together, so A is read from HBM once and
+// each B tile once per group.
 // Every wait is bounded (error flag g_tc4_error, no hang).
 #include "common.cuh"
 #include "kernels.h"
 
 #include <cuda.h>   // CUtensorMap and its enums (types only; the encoder comes from the runtime)
 
+#include <atomic>
+
 namespace p2c {
 
 #define T4_BM 128
-#define T4_BN 256
 #define T4_KB 128
-#define T4_NST 4
+#define T4_TR 8           // ring of published tile numbers
+#define T4_NO_TILE 0xFFFFFFFFu
+#define T4_ACC_STRIDE 256 // TMEM columns between the two accumulators
+#define T4_SFA_COL 448    // TMEM columns of the scale factors (A, then B)
+#define T4_SFB_COL 480
 #define T4_STAGE_A (T4_BM * T4_KB)
-#define T4_STAGE_B (T4_BN * T4_KB)
-#define T4_STAGE (T4_STAGE_A + T4_STAGE_B)
+#define T4_RCOMMON 48     // recovery padding of B: a multiple of both tiles' slice counts
+
+// The two tile shapes: 256 bit rows (16 recovery slices) with one TMEM
+// accumulator and a 4-stage ring (the default), or 192 bit rows (12 slices)
+// with two accumulators (the next tile's MMAs overlap the read-out) and a
+// 5-stage ring (selectable; measured slower, see tc4_shape_for).
+template<int BN> struct T4Shape {
+	static constexpr int RPT = BN / 16;
+	static constexpr int NACC = BN <= 192 ? 2 : 1;
+	static constexpr int NST = BN <= 192 ? 5 : 4;
+	static constexpr int STAGE = T4_STAGE_A + BN * T4_KB;
+	// mbarriers after the stages
+	static constexpr int BAR_FULL = 0;                  // [NST] a stage's operands landed
+	static constexpr int BAR_EMPTY = NST;               // [NST] a stage's MMAs completed
+	static constexpr int BAR_TFULL = 2 * NST;           // [2] an accumulator holds a finished tile
+	static constexpr int BAR_TEMPTY = 2 * NST + 2;      // [2] the epilogue has read it (4 arrivals)
+	static constexpr int BAR_IDFULL = 2 * NST + 4;      // [TR] a tile number was published
+	static constexpr int BAR_IDEMPTY = BAR_IDFULL + T4_TR; // [TR] its readers have read it (5 arrivals)
+	static constexpr int BAR_DRAIN = BAR_IDEMPTY + T4_TR;
+	static constexpr int NBARS = BAR_DRAIN + 1;
+	static constexpr size_t SMEM = (size_t)NST * STAGE + NBARS * 8 + (T4_TR + 2) * 4 + 1024;
+	static_assert(NACC == 1 || T4_ACC_STRIDE + BN <= T4_SFA_COL, "accumulators overlap the scale factors");
+	static_assert(BN <= T4_SFA_COL, "accumulator overlaps the scale factors");
+	static_assert(SMEM <= 227 * 1024, "shared memory");
+};
 #define T4_WAIT (1u << 24)
 #define T4_THREADS 192
 #define T4_A_CHUNK_BYTES (1ull << 30)
@@ -126,6 +157,10 @@ __device__ __forceinline__ bool t4_wait(uint32_t bar, uint32_t parity) {
 	return false;
 }
 
+__device__ __forceinline__ void t4_arrive(uint32_t bar) {
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" :: "r"(bar) : "memory");
+}
+
 // K-major operand in shared memory, 128-byte swizzle: 8-row atoms 1024 bytes apart
 __device__ __forceinline__ uint64_t t4_desc(uint32_t saddr) {
 	uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
@@ -138,8 +173,8 @@ __device__ __forceinline__ uint64_t t4_desc(uint32_t saddr) {
 
 // instruction descriptor of the block-scaled kinds: A and B e2m1 (mxf4 code
 // 1), K-major, N >> 3, ue8m0 scale factors, M >> 4, scale-factor ids 0
-__device__ __forceinline__ uint32_t t4_idesc() {
-	return (1u << 7) | (1u << 10) | ((uint32_t)(T4_BN >> 3) << 17) | (1u << 23) | ((uint32_t)(T4_BM >> 4) << 24);
+template<int BN> __device__ __forceinline__ uint32_t t4_idesc() {
+	return (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | (1u << 23) | ((uint32_t)(T4_BM >> 4) << 24);
 }
 
 // tile t -> (word tile mt, recovery tile nt): groups of groupM word tiles walk
@@ -168,42 +203,48 @@ __device__ __forceinline__ bool t4_wait_ab(uint32_t bar, uint32_t parity, volati
 	return false;
 }
 
-// Persistent GEMM: one CTA per SM walks the tiles blockIdx.x, blockIdx.x +
-// gridDim.x, ... in raster order.  Warp 0 (one thread) streams both
-// operands' k-blocks of its tiles through the ring without stopping at tile
-// boundaries; warp 1 (one thread) issues the MMAs, and before the first MMA of
-// a tile waits until the epilogue has read the previous tile's accumulators
-// out of TMEM; warps 2-5 (each the TMEM lane quarter warp % 4) are the
-// epilogue.  So the ring refills while a tile's results are written, and the
-// per-CTA set-up (barriers, TMEM allocation, scale factors) is paid once per
-// SM instead of once per tile.
+// Persistent GEMM: one CTA per SM.  Warp 0 (one thread) takes tiles from a
+// global counter (tile = atomicAdd(counter) - tileBase, so an SM that another
+// kernel holds for a while simply takes fewer tiles), publishes each tile
+// number in a ring of TR slots, and streams the tile's k-blocks through the
+// stage ring without stopping at tile boundaries; warp 1 (one thread) reads
+// the tile numbers and issues the MMAs of tile j into TMEM accumulator
+// j % NACC, first waiting until the epilogue has read that accumulator's
+// previous tile; warps 2-5 (each the TMEM lane quarter warp % 4) read the tile
+// numbers and the accumulators out of TMEM.  With two accumulators the MMAs
+// of the next tile run while the epilogue writes the previous one.  Each CTA's producer
+// does exactly one counter fetch beyond its last tile (the one that ends
+// it), so a launch advances the counter by tiles + CTAs.
+template<int BN>
 __global__ void __launch_bounds__(T4_THREADS, 1) k_tc4_gemm(const __grid_constant__ CUtensorMap tmA,
                                                           const __grid_constant__ CUtensorMap tmB,
                                                           uint16_t* __restrict__ rec, size_t recPitch, unsigned R,
                                                           unsigned kBlocks, unsigned mTiles, unsigned nTiles,
-                                                          unsigned groupM, size_t w0, size_t nWords, int accumulate)
+                                                          unsigned groupM, size_t w0, size_t nWords, int accumulate,
+                                                          unsigned* __restrict__ tileCounter, unsigned tileBase)
 {
+	typedef T4Shape<BN> Sh;
+	constexpr int NST = Sh::NST, STAGE = Sh::STAGE, NACC = Sh::NACC;
 	extern __shared__ __align__(1024) uint8_t smem_raw[];
 	const uint32_t raw = t4_saddr(smem_raw);
 	const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
 	uint8_t* sm = smem_raw + pad;
 	const uint32_t sbase = raw + pad;
-	// full[NST], empty[NST], tmemFull, tmemEmpty, drain
-	const uint32_t barBase = sbase + T4_NST * T4_STAGE;
-	const uint32_t tmemFull = barBase + 8u * (2 * T4_NST), tmemEmpty = tmemFull + 8u, drainBar = tmemFull + 16u;
-	uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + T4_NST * T4_STAGE + (2 * T4_NST + 3) * 8);
+	const uint32_t barBase = sbase + NST * STAGE;
+	auto bar = [&](int k) -> uint32_t { return barBase + 8u * (uint32_t)k; };
+	volatile uint32_t* tileIds = reinterpret_cast<volatile uint32_t*>(sm + NST * STAGE + Sh::NBARS * 8);
+	uint32_t* tslot = const_cast<uint32_t*>(tileIds) + T4_TR;
 	volatile uint32_t* abortFlag = tslot + 1;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const unsigned nAll = mTiles * nTiles;
 
 	if(threadIdx.x == 0) {
-		for(int s = 0; s < T4_NST; s++) {
-			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barBase + 8u * s) : "memory");
-			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barBase + 8u * (T4_NST + s)) : "memory");
+		for(int k = 0; k < Sh::NBARS; k++) {
+			unsigned count = 1;
+			if(k == Sh::BAR_TEMPTY || k == Sh::BAR_TEMPTY + 1) count = 4;
+			if(k >= Sh::BAR_IDEMPTY && k < Sh::BAR_IDEMPTY + T4_TR) count = 5;
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar(k)), "r"(count) : "memory");
 		}
-		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(tmemFull) : "memory");
-		asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" :: "r"(tmemEmpty) : "memory");
-		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(drainBar) : "memory");
 		*abortFlag = 0u;
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		asm volatile("prefetch.tensormap [%0];" :: "l"(&tmA) : "memory");
@@ -218,16 +259,17 @@ __global__ void __launch_bounds__(T4_THREADS, 1) k_tc4_gemm(const __grid_constan
 	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 	const uint32_t tmem = *tslot;
 
-	// scale factors: TMEM columns 256-511 of every lane hold ue8m0 1.0 bytes;
-	// each epilogue warp fills its own lane quarter
+	// scale factors: TMEM columns 448-511 of every lane hold ue8m0 1.0 bytes
+	// (A's at column 448, B's at 480); each epilogue warp fills its own lane
+	// quarter
 	if(warp >= 2) {
 		const uint32_t one = 0x7F7F7F7Fu;
 		const uint32_t lane0 = (uint32_t)(32 * (warp & 3)) << 16;
 #pragma unroll
-		for(int q = 0; q < 8; q++)
+		for(int q = 0; q < 2; q++)
 			asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
 			             "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};"
-			             :: "r"(tmem + lane0 + 256 + 32 * q), "r"(one) : "memory");
+			             :: "r"(tmem + lane0 + T4_SFA_COL + 32 * q), "r"(one) : "memory");
 		asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -236,86 +278,108 @@ __global__ void __launch_bounds__(T4_THREADS, 1) k_tc4_gemm(const __grid_constan
 
 	if(warp == 0) {
 		if(lane == 0) {
-			// TMA producer: k-block g of the CTA's sequence goes to stage g % NST
+			// producer: tile numbers, then k-block g of the CTA's sequence into stage g % NST
 			uint32_t g = 0;
 			bool ok = true;
-			for(unsigned t = blockIdx.x; t < nAll && ok; t += gridDim.x) {
+			for(uint32_t j = 0; ok; j++) {
+				const unsigned slot = j % T4_TR;
+				if(j >= T4_TR && !t4_wait_ab(bar(Sh::BAR_IDEMPTY + slot), ((j / T4_TR) - 1) & 1, abortFlag)) {
+					ok = false;
+					break;
+				}
+				const unsigned t = atomicAdd(tileCounter, 1u) - tileBase;
+				const bool more = t < nAll;
+				tileIds[slot] = more ? t : T4_NO_TILE;
+				t4_arrive(bar(Sh::BAR_IDFULL + slot));
+				if(!more) break;
 				unsigned mt, nt;
 				t4_tile(t, mTiles, nTiles, groupM, mt, nt);
 				for(unsigned kb = 0; kb < kBlocks; kb++, g++) {
-					const unsigned s = g % T4_NST;
-					if(g >= T4_NST && !t4_wait_ab(barBase + 8u * (T4_NST + s), ((g / T4_NST) - 1) & 1, abortFlag)) {
+					const unsigned s = g % NST;
+					if(g >= NST && !t4_wait_ab(bar(Sh::BAR_EMPTY + s), ((g / NST) - 1) & 1, abortFlag)) {
 						ok = false;
 						break;
 					}
-					const uint32_t full = barBase + 8u * s;
-					const uint32_t dA = sbase + s * T4_STAGE, dB = dA + T4_STAGE_A;
+					const uint32_t full = bar(Sh::BAR_FULL + s);
+					const uint32_t dA = sbase + s * STAGE, dB = dA + T4_STAGE_A;
 					asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
-					             :: "r"(full), "r"((uint32_t)T4_STAGE) : "memory");
+					             :: "r"(full), "r"((uint32_t)STAGE) : "memory");
 					const int x = (int)(kb * T4_KB);
 					asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
 					             :: "r"(dA), "l"(&tmA), "r"(x), "r"((int)(mt * T4_BM)), "r"(full) : "memory");
 					asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-					             :: "r"(dB), "l"(&tmB), "r"(x), "r"((int)(nt * T4_BN)), "r"(full) : "memory");
+					             :: "r"(dB), "l"(&tmB), "r"(x), "r"((int)(nt * BN)), "r"(full) : "memory");
 				}
 			}
 			if(!ok) {
 				// let the copies still in flight land before the CTA ends
-				for(uint32_t h = g > T4_NST ? g - T4_NST : 0; h < g; h++)
-					t4_wait(barBase + 8u * (h % T4_NST), (h / T4_NST) & 1);
+				for(uint32_t h = g > NST ? g - NST : 0; h < g; h++)
+					t4_wait(bar(Sh::BAR_FULL + h % NST), (h / NST) & 1);
 			}
 		}
 	} else if(warp == 1) {
 		if(lane == 0) {
-			// MMA issuer
-			const uint32_t idesc = t4_idesc();
-			const uint32_t sfa = tmem + 256, sfb = tmem + 384;
-			uint32_t g = 0, i = 0;
+			// MMA issuer: tile j accumulates in TMEM columns (j % NACC) * 256 ..
+			const uint32_t idesc = t4_idesc<BN>();
+			const uint32_t sfa = tmem + T4_SFA_COL, sfb = tmem + T4_SFB_COL;
+			uint32_t g = 0;
 			bool ok = true;
-			for(unsigned t = blockIdx.x; t < nAll && ok; t += gridDim.x, i++) {
-				// the epilogue has read the previous tile's accumulators
-				if(i > 0 && !t4_wait_ab(tmemEmpty, (i - 1) & 1, abortFlag)) { ok = false; break; }
+			for(uint32_t j = 0; ok; j++) {
+				const unsigned slot = j % T4_TR;
+				if(!t4_wait_ab(bar(Sh::BAR_IDFULL + slot), (j / T4_TR) & 1, abortFlag)) { ok = false; break; }
+				const unsigned t = tileIds[slot];
+				t4_arrive(bar(Sh::BAR_IDEMPTY + slot));
+				if(t == T4_NO_TILE) break;
+				const unsigned buf = j % NACC, use = j / NACC;
+				// the epilogue has read this accumulator's previous tile
+				if(use >= 1 && !t4_wait_ab(bar(Sh::BAR_TEMPTY + buf), (use - 1) & 1, abortFlag)) { ok = false; break; }
 				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				const uint32_t dacc = tmem + buf * T4_ACC_STRIDE;
 				for(unsigned kb = 0; kb < kBlocks; kb++, g++) {
-					const unsigned s = g % T4_NST;
-					if(!t4_wait_ab(barBase + 8u * s, (g / T4_NST) & 1, abortFlag)) { ok = false; break; }
+					const unsigned s = g % NST;
+					if(!t4_wait_ab(bar(Sh::BAR_FULL + s), (g / NST) & 1, abortFlag)) { ok = false; break; }
 					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-					const uint32_t aS = sbase + s * T4_STAGE, bS = aS + T4_STAGE_A;
+					const uint32_t aS = sbase + s * STAGE, bS = aS + T4_STAGE_A;
 #pragma unroll
 					for(int k = 0; k < 4; k++) {
 						const uint64_t ad = t4_desc(aS + k * 32), bd = t4_desc(bS + k * 32);
 						const uint32_t acc = (kb | k) != 0;
 						asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
 						             "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], [%5], p;\n\t}"
-						             :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(sfa), "r"(sfb), "r"(acc) : "memory");
+						             :: "r"(dacc), "l"(ad), "l"(bd), "r"(idesc), "r"(sfa), "r"(sfb), "r"(acc) : "memory");
 					}
 					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-					             :: "r"(barBase + 8u * (T4_NST + s)) : "memory");
+					             :: "r"(bar(Sh::BAR_EMPTY + s)) : "memory");
 				}
 				if(ok)
 					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-					             :: "r"(tmemFull) : "memory");
+					             :: "r"(bar(Sh::BAR_TFULL + buf)) : "memory");
 			}
 			// every MMA this thread issued has completed before TMEM is freed
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-			             :: "r"(drainBar) : "memory");
-			t4_wait(drainBar, 0);
+			             :: "r"(bar(Sh::BAR_DRAIN)) : "memory");
+			t4_wait(bar(Sh::BAR_DRAIN), 0);
 		}
 	} else {
 		// epilogue: thread (warp, lane) owns word mt*128 + 32*(warp%4) + lane
-		// and the 256 accumulator columns of its TMEM lane = 16 recovery words
+		// and the BN accumulator columns of its TMEM lane = BN / 16 recovery words
 		const unsigned quarter = warp & 3;
 		const uint32_t lane0 = (uint32_t)(32 * quarter) << 16;
-		uint32_t i = 0;
-		for(unsigned t = blockIdx.x; t < nAll; t += gridDim.x, i++) {
+		for(uint32_t j = 0;; j++) {
+			const unsigned slot = j % T4_TR;
+			if(!__all_sync(0xffffffffu, t4_wait_ab(bar(Sh::BAR_IDFULL + slot), (j / T4_TR) & 1, abortFlag))) break;
+			const unsigned t = tileIds[slot];
+			__syncwarp();
+			if(lane == 0) t4_arrive(bar(Sh::BAR_IDEMPTY + slot));
+			if(t == T4_NO_TILE) break;
 			unsigned mt, nt;
 			t4_tile(t, mTiles, nTiles, groupM, mt, nt);
-			const bool ok = __all_sync(0xffffffffu, t4_wait_ab(tmemFull, i & 1, abortFlag));
-			if(!ok) break;
+			const unsigned buf = j % NACC, use = j / NACC;
+			if(!__all_sync(0xffffffffu, t4_wait_ab(bar(Sh::BAR_TFULL + buf), use & 1, abortFlag))) break;
 			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 			const size_t w = w0 + (size_t)mt * T4_BM + 32 * quarter + lane;
 #pragma unroll 1
-			for(int q = 0; q < 8; q++) {
+			for(int q = 0; q < BN / 32; q++) {
 				uint32_t v[32];
 				asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
 				             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -324,7 +388,7 @@ __global__ void __launch_bounds__(T4_THREADS, 1) k_tc4_gemm(const __grid_constan
 				               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
 				               "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
 				               "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-				             : "r"(tmem + lane0 + 32 * q));
+				             : "r"(tmem + lane0 + buf * T4_ACC_STRIDE + 32 * q));
 				asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 				// parity of an exact integer n < 2^23 held in fp32: n + 2^23 has
 				// unit ulp, so bit 0 of its encoding is bit 0 of n (one full-rate
@@ -335,7 +399,7 @@ __global__ void __launch_bounds__(T4_THREADS, 1) k_tc4_gemm(const __grid_constan
 					word0 |= (__float_as_uint(__fadd_rn(__uint_as_float(v[c]), 8388608.0f)) & 1u) << c;
 					word1 |= (__float_as_uint(__fadd_rn(__uint_as_float(v[16 + c]), 8388608.0f)) & 1u) << c;
 				}
-				const unsigned r0 = nt * 16 + 2 * q;
+				const unsigned r0 = nt * Sh::RPT + 2 * q;
 				if(w < nWords) {
 					if(r0 < R) {
 						uint16_t* p = rec + (size_t)r0 * recPitch + w;
@@ -347,10 +411,10 @@ __global__ void __launch_bounds__(T4_THREADS, 1) k_tc4_gemm(const __grid_constan
 					}
 				}
 			}
-			// this warp's TMEM reads are done: the next tile's MMAs may start
+			// this warp's TMEM reads are done: the accumulator may take a new tile
 			asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 			__syncwarp();
-			if(lane == 0) asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" :: "r"(tmemEmpty) : "memory");
+			if(lane == 0) t4_arrive(bar(Sh::BAR_TEMPTY + buf));
 		}
 	}
 	__syncwarp();
@@ -392,13 +456,39 @@ static int t4_map(CUtensorMap* m, const void* base, size_t rowBytes, size_t rows
 	return 0;
 }
 
+// scratch: [tile counter, 1 KiB] [B: 16 x roundup(R, 48) rows of kBytes] [A chunk]
+#define T4_HDR_BYTES 1024
 static size_t t4_kbytes(unsigned nIn) { return (size_t)round_up(nIn ? nIn : 1, 16) * 8; }
-static size_t t4_bbytes(unsigned R, unsigned nIn) { return (size_t)round_up(R ? R : 1, 16) * 16 * t4_kbytes(nIn); }
+static unsigned t4_rpad(unsigned R) { return (unsigned)round_up(R ? R : 1, T4_RCOMMON); }
+
+static std::atomic<int> g_tc4_shape{0};
+int set_tc4_shape(int shape) { return g_tc4_shape.exchange(shape); }
+
+// Tile shape for kBlocks k-blocks (16 inputs each) per tile.  The 192-row
+// tile with two accumulators hides each tile's read-out behind the next
+// tile's MMAs, but its A tiles are loaded 4/3 as often per MMA and its MMAs
+// are narrower; measured on GB300 it is slower on every shape tried (4096 x
+// 4096 x 256 KiB: 187.6 against 146.5 ms; 512 x 192 x 512 KiB: 2.72 against
+// 2.32 ms; 2000 x 200 x 2 MiB: 42.6 against 35.6 ms; 1000 x 100 x 1 MiB:
+// 6.51 against 5.67 ms), so the automatic choice is the 256-row tile.
+int tc4_shape_for(unsigned kBlocks) {
+	(void)kBlocks;
+	const int s = g_tc4_shape.load();
+	return s == 2 ? 2 : 1;
+}
+static size_t t4_bbytes(unsigned R, unsigned nIn) {
+	return round_up((size_t)t4_rpad(R) * 16 * t4_kbytes(nIn), 1024);
+}
 
 size_t tc4_scratch_bytes(unsigned R, unsigned nIn, size_t nWords) {
 	const size_t aFull = round_up(nWords ? nWords : 1, T4_BM) * t4_kbytes(nIn);
 	const size_t aMax = std::max<size_t>(T4_A_CHUNK_BYTES, (size_t)T4_BM * t4_kbytes(nIn));
-	return round_up(t4_bbytes(R, nIn), 1024) + round_up(std::min(aFull, aMax), 1024);
+	return T4_HDR_BYTES + t4_bbytes(R, nIn) + round_up(std::min(aFull, aMax), 1024);
+}
+
+size_t tc4_scratch_chunked_bytes(unsigned R, unsigned nIn, size_t nWords, size_t aChunkBytes) {
+	const size_t aMin = std::max<size_t>(aChunkBytes, (size_t)T4_BM * t4_kbytes(nIn));
+	return std::min(tc4_scratch_bytes(R, nIn, nWords), T4_HDR_BYTES + t4_bbytes(R, nIn) + round_up(aMin, 1024));
 }
 
 int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec, size_t recPitch,
@@ -416,34 +506,43 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 		return -1;
 	}
 	const size_t kBytes = t4_kbytes(nIn);
-	const unsigned nInPad = (unsigned)(kBytes / 8), rPad = (unsigned)round_up(R, 16);
-	const size_t bBytes = round_up(t4_bbytes(R, nIn), 1024);
-	if(!scratch || scratchBytes < bBytes + (size_t)T4_BM * kBytes) {
-		set_error("tensor method (mxf4) needs at least %zu bytes of scratch, %zu given", bBytes + (size_t)T4_BM * kBytes,
-		          scratchBytes);
+	const unsigned nInPad = (unsigned)(kBytes / 8), rPad = t4_rpad(R);
+	const size_t bBytes = t4_bbytes(R, nIn);
+	const size_t minBytes = T4_HDR_BYTES + bBytes + (size_t)T4_BM * kBytes;
+	if(!scratch || scratchBytes < minBytes) {
+		set_error("tensor method (mxf4) needs at least %zu bytes of scratch, %zu given", minBytes, scratchBytes);
 		return -1;
 	}
-	uint8_t* B = reinterpret_cast<uint8_t*>(scratch);
+	unsigned* counter = reinterpret_cast<unsigned*>(scratch);
+	uint8_t* B = reinterpret_cast<uint8_t*>(scratch) + T4_HDR_BYTES;
 	uint8_t* A = B + bBytes;
 	// words per chunk: what the rest of the scratch holds, in whole 128-word tiles
-	size_t wChunk = (scratchBytes - bBytes) / kBytes / T4_BM * T4_BM;
+	size_t wChunk = (scratchBytes - T4_HDR_BYTES - bBytes) / kBytes / T4_BM * T4_BM;
 	wChunk = std::min(wChunk, round_up(nWords, T4_BM));
 	const size_t nB = (size_t)rPad * nInPad;
 	k_tc4_prep_coeff<<<(unsigned)((nB + 255) / 256), 256, 0, st>>>(coeff, R, nIn, rPad, nInPad, B);
 	P2C_CUDA_TRY(cudaGetLastError());
+	const unsigned kBlocks = (unsigned)(kBytes / T4_KB);
+	const int shape = tc4_shape_for(kBlocks);
+	const unsigned bn = shape == 1 ? 256 : 192, rpt = bn / 16;
+	const size_t smem = shape == 1 ? T4Shape<256>::SMEM : T4Shape<192>::SMEM;
+	if(shape == 1) P2C_CUDA_TRY(cudaFuncSetAttribute(k_tc4_gemm<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	else P2C_CUDA_TRY(cudaFuncSetAttribute(k_tc4_gemm<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	CUtensorMap tmB;
-	if(t4_map(&tmB, B, kBytes, (size_t)rPad * 16, T4_BN)) return -1;
-	const size_t smem = T4_NST * T4_STAGE + (2 * T4_NST + 3) * 8 + 16 + 1024;
-	P2C_CUDA_TRY(cudaFuncSetAttribute(k_tc4_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	if(t4_map(&tmB, B, kBytes, (size_t)rPad * 16, bn)) return -1;
 	int dev = 0, nSM = 0;
 	P2C_CUDA_TRY(cudaGetDevice(&dev));
 	P2C_CUDA_TRY(cudaDeviceGetAttribute(&nSM, cudaDevAttrMultiProcessorCount, dev));
-	const unsigned nTiles = rPad / 16;
-	const unsigned kBlocks = (unsigned)(kBytes / T4_KB);
+	// recovery tiles: B has rows for rPad >= nTiles * rpt slices
+	const unsigned nTiles = (R + rpt - 1) / rpt;
 	// word tiles per raster group: their A tiles (128 x kBytes each) stay in
 	// L2 (about 48 MiB of it) while the group walks the recovery tiles, so A
 	// is read from HBM once and each B tile once per group
 	const unsigned groupM = (unsigned)std::min<size_t>(64, std::max<size_t>(8, (48ull << 20) / ((size_t)T4_BM * kBytes)));
+	// the tile counter starts at 0 for this call; each launch advances it by
+	// its tiles + CTAs (every CTA's last fetch finds no tile)
+	P2C_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+	unsigned base = 0;
 	for(size_t w0 = 0; w0 < nWords; w0 += wChunk) {
 		const size_t rows = std::min(wChunk, round_up(nWords - w0, T4_BM));
 		dim3 pg((unsigned)(rows / 64), (nInPad + 63) / 64);
@@ -452,18 +551,24 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 		CUtensorMap tmA;
 		if(t4_map(&tmA, A, kBytes, rows, T4_BM)) return -1;
 		const unsigned mTiles = (unsigned)(rows / T4_BM);
-		// one CTA per SM (its shared memory allows no second), each walking tiles
-		const unsigned grid = (unsigned)std::min<size_t>((size_t)mTiles * nTiles, (size_t)std::max(nSM, 1));
-		k_tc4_gemm<<<grid, T4_THREADS, smem, st>>>(tmA, tmB, rec, recPitch, R, kBlocks, mTiles, nTiles, groupM, w0, nWords,
-		                                               accumulate);
+		const unsigned nAll = mTiles * nTiles;
+		// one CTA per SM (its shared memory allows no second)
+		const unsigned grid = (unsigned)std::min<size_t>((size_t)nAll, (size_t)std::max(nSM, 1));
+		if(shape == 1)
+			k_tc4_gemm<256><<<grid, T4_THREADS, smem, st>>>(tmA, tmB, rec, recPitch, R, kBlocks, mTiles, nTiles, groupM, w0,
+			                                                nWords, accumulate, counter, base);
+		else
+			k_tc4_gemm<192><<<grid, T4_THREADS, smem, st>>>(tmA, tmB, rec, recPitch, R, kBlocks, mTiles, nTiles, groupM, w0,
+			                                                nWords, accumulate, counter, base);
 		P2C_CUDA_TRY(cudaGetLastError());
+		base += nAll + grid;
 	}
 	return 0;
 }
 
 // ------------------------------------------------------------------ peak
 // Calibration of the roofline denominator: one CTA per SM issues `iters`
-// MMAs of the GEMM's shape (M=128, N=256, K=64, kind::mxf4, unit scales) on
+// MMAs of the default tile shape (M=128, N=256, K=64, kind::mxf4, unit scales) on
 // operands resident in shared memory, back to back into one accumulator, and
 // waits (bounded) for their completion.  No global memory traffic: the rate
 // is the tensor pipe's for this instruction.
@@ -474,10 +579,11 @@ __global__ void __launch_bounds__(128, 1) k_tc4_mma_rate(unsigned iters)
 	const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
 	uint8_t* sm = smem_raw + pad;
 	const uint32_t sbase = raw + pad;
-	const uint32_t doneBar = sbase + T4_STAGE;
-	uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + T4_STAGE + 8);
+	constexpr int STAGE = T4Shape<256>::STAGE;
+	const uint32_t doneBar = sbase + STAGE;
+	uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + STAGE + 8);
 	const int warp = threadIdx.x >> 5;
-	for(int e = threadIdx.x; e < T4_STAGE / 16; e += 128) reinterpret_cast<uint4*>(sm)[e] = make_uint4(0, 0, 0, 0);
+	for(int e = threadIdx.x; e < STAGE / 16; e += 128) reinterpret_cast<uint4*>(sm)[e] = make_uint4(0, 0, 0, 0);
 	if(threadIdx.x == 0) {
 		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(doneBar) : "memory");
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -495,23 +601,23 @@ __global__ void __launch_bounds__(128, 1) k_tc4_mma_rate(unsigned iters)
 		const uint32_t one = 0x7F7F7F7Fu;
 		const uint32_t lane0 = (uint32_t)(32 * warp) << 16;
 #pragma unroll
-		for(int q = 0; q < 8; q++)
+		for(int q = 0; q < 2; q++)
 			asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
 			             "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};"
-			             :: "r"(tmem + lane0 + 256 + 32 * q), "r"(one) : "memory");
+			             :: "r"(tmem + lane0 + T4_SFA_COL + 32 * q), "r"(one) : "memory");
 		asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 	__syncthreads();
 	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 	if(threadIdx.x == 0) {
-		const uint32_t idesc = t4_idesc();
+		const uint32_t idesc = t4_idesc<256>();
 		const uint64_t ad = t4_desc(sbase), bd = t4_desc(sbase + T4_STAGE_A);
 		for(unsigned it = 0; it < iters; it++) {
 			const uint32_t acc = it != 0;
 			asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
 			             "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], [%5], p;\n\t}"
-			             :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(tmem + 256), "r"(tmem + 384), "r"(acc) : "memory");
+			             :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(tmem + T4_SFA_COL), "r"(tmem + T4_SFB_COL), "r"(acc) : "memory");
 		}
 		asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(doneBar) : "memory");
 	}
@@ -527,7 +633,7 @@ int tc4_mma_rate(double* macsPerSec, cudaStream_t st) {
 	int dev = 0, sms = 0;
 	P2C_CUDA_TRY(cudaGetDevice(&dev));
 	P2C_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-	const size_t smem = T4_STAGE + 8 + 16 + 1024;
+	const size_t smem = T4Shape<256>::STAGE + 8 + 16 + 1024;
 	P2C_CUDA_TRY(cudaFuncSetAttribute(k_tc4_mma_rate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const unsigned iters = 20000;
 	cudaEvent_t e0, e1;
@@ -546,7 +652,7 @@ int tc4_mma_rate(double* macsPerSec, cudaStream_t st) {
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
 	P2C_CUDA_TRY(cudaGetLastError());
-	*macsPerSec = best > 0.f ? (double)iters * sms * T4_BM * T4_BN * 64 / (best * 1e-3) : 0.0;
+	*macsPerSec = best > 0.f ? (double)iters * sms * T4_BM * 256 * 64 / (best * 1e-3) : 0.0;
 	return 0;
 }
 

@@ -95,8 +95,12 @@ int file_md5_staged(const void* rows, size_t pitchBytes, unsigned nFiles, const 
 int hash_error_take();
 // block-scaled 4-bit tcgen05 form (k_tc4.cu)
 size_t tc4_scratch_bytes(unsigned R, unsigned nIn, size_t nWords);
+// scratch for word chunks of at most aChunkBytes of expanded input planes
+size_t tc4_scratch_chunked_bytes(unsigned R, unsigned nIn, size_t nWords, size_t aChunkBytes);
 int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec, size_t recPitch,
                unsigned R, size_t nWords, int accumulate, void* scratch, size_t scratchBytes, cudaStream_t st);
 int tc4_error_take();
 int tc4_mma_rate(double* macsPerSec, cudaStream_t st);
+int set_tc4_shape(int shape);
+int tc4_shape_for(unsigned kBlocks);
 } // namespace p2c

@@ -11,9 +11,10 @@ from parpar_gb300 import _lib, synth
 pytestmark = pytest.mark.gpu
 
 
-def run_fp4(n, R, S, seed, accumulate=False, scratch_bytes=None):
+def run_fp4(n, R, S, seed, accumulate=False, scratch_bytes=None, shape=0):
     import torch
     L = _lib.load()
+    prev = L.par2cuda_set_tc4_shape(shape)
     pitch = L.par2cuda_row_pitch_bytes(S)
     pw = pitch // 2
     x = synth.slices(seed, 0, n, S)
@@ -27,8 +28,11 @@ def run_fp4(n, R, S, seed, accumulate=False, scratch_bytes=None):
     nw = S // 2
     sb = scratch_bytes or L.par2cuda_tensor_fp4_scratch_bytes(R, n, nw)
     scratch = torch.empty(sb, dtype=torch.uint8, device="cuda")
-    rc = L.par2cuda_muladd(d_in.data_ptr(), pw, n, d_coeff.data_ptr(), d_rec.data_ptr(), pw, R, nw, int(accumulate),
-                           _lib.METHOD_TENSOR_FP4, scratch.data_ptr(), sb, None)
+    try:
+        rc = L.par2cuda_muladd(d_in.data_ptr(), pw, n, d_coeff.data_ptr(), d_rec.data_ptr(), pw, R, nw, int(accumulate),
+                               _lib.METHOD_TENSOR_FP4, scratch.data_ptr(), sb, None)
+    finally:
+        L.par2cuda_set_tc4_shape(prev)
     assert rc == 0, L.par2cuda_last_error()
     torch.cuda.synchronize()
     assert L.par2cuda_device_error() == 0
@@ -39,25 +43,33 @@ def run_fp4(n, R, S, seed, accumulate=False, scratch_bytes=None):
     return got, want
 
 
+@pytest.mark.parametrize("shape", [1, 2])
 @pytest.mark.parametrize("n,R,S", [
-    (16, 16, 256),        # one 128-word x 16-slice tile, one K block
+    (16, 12, 256),        # one 128-word x 12-slice tile, one K block
+    (16, 16, 256),        # one 16-slice tile; two 12-slice tiles, the second padded
     (3, 2, 256),          # padded inputs and recovery slices
     (37, 20, 10000),      # two recovery tiles, ragged words
     (200, 33, 65536),     # several K blocks, three recovery tiles
+    (40, 100, 131072),    # 7 or 9 recovery tiles x 512 word tiles: accumulators reused, many tiles per CTA
+    (1100, 30, 20000),    # 69 k-blocks (the automatic choice takes the 16-slice tile)
 ])
-def test_fp4_matches_oracle(n, R, S):
-    got, want = run_fp4(n, R, S, seed=n * 31 + R)
+def test_fp4_matches_oracle(n, R, S, shape):
+    got, want = run_fp4(n, R, S, seed=n * 31 + R, shape=shape)
     assert np.array_equal(got, want)
 
 
-def test_fp4_accumulate_and_word_chunks():
+@pytest.mark.parametrize("shape", [1, 2])
+def test_fp4_accumulate_and_word_chunks(shape):
     from parpar_gb300 import _lib as lib
     L = lib.load()
     n, R, S = 48, 24, 40000
     kbytes = ((n + 15) // 16 * 16) * 8
-    bbytes = ((R + 15) // 16 * 16) * 16 * kbytes
+    one_tile = (128 * kbytes + 1023) // 1024 * 1024
+    # the scratch for one 128-word tile, less that tile: the tile counter and
+    # the coefficient bit matrix
+    fixed = L.par2cuda_tensor_fp4_scratch_bytes(R, n, 1) - one_tile
     # room for 2 tiles of words only: 40000-byte rows take 79 chunks
-    small = (bbytes + 1023) // 1024 * 1024 + 2 * 128 * kbytes
-    got, want = run_fp4(n, R, S, seed=5, accumulate=True, scratch_bytes=small)
+    small = fixed + 2 * 128 * kbytes
+    got, want = run_fp4(n, R, S, seed=5, accumulate=True, scratch_bytes=small, shape=shape)
     assert np.array_equal(got, want)
     assert L.par2cuda_tensor_fp4_scratch_bytes(R, n, S // 2) >= small
