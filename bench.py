@@ -458,7 +458,8 @@ def single_job_measure(args, cfg, file_lens, job, steps, warmup, e2e=True):
     out = {"ms_per_job": t0.elapsed_time(t1) / steps, "jobs": steps,
            "muladd_ms": float(np.mean([e[0].elapsed_time(e[1]) for e in ev])),
            "file_md5_ms": float(np.mean([e[2].elapsed_time(e[3]) for e in ev])) if cfg["hashes"] else 0.0,
-           "launches_per_job": 6 + (2 if cfg["hashes"] else 0)}
+           "launches_per_job": 4 + L.par2cuda_muladd_launches(R, N, job.row_words, job.method, job.scratch_bytes) +
+                               (2 if cfg["hashes"] else 0)}
     out["value"] = N * R * (S // 2) / (out["ms_per_job"] / 1e3)
     if e2e:
         host_in = torch.empty((N, S), dtype=torch.uint8, pin_memory=True)

@@ -53,7 +53,7 @@ enum { PAR2CUDA_ADD_OK = 0, PAR2CUDA_ADD_OK_BUSY = 1, PAR2CUDA_ADD_FULL = 2 };
 enum {
 	PAR2CUDA_METHOD_AUTO = 0,
 	PAR2CUDA_METHOD_COMB = 1,   /* shared-memory XOR-combination tables (default) */
-	PAR2CUDA_METHOD_XOR = 2,    /* LOP3, per-coefficient-bit masks */
+	PAR2CUDA_METHOD_XOR = 2,    /* LOP3 over 16 bit planes (per-coefficient-bit masks) */
 	PAR2CUDA_METHOD_NIBBLE = 3, /* shared-memory split-nibble tables */
 	PAR2CUDA_METHOD_TENSOR = 4, /* tcgen05 GF(2) bit-matrix product (e4m3 0/1, fp32 accumulators) */
 	PAR2CUDA_METHOD_TENSOR_FP4 = 5 /* tcgen05 block-scaled 4-bit (mxf4) GF(2) product, TMA-fed; device level only */
@@ -220,6 +220,11 @@ size_t par2cuda_tensor_fp4_scratch_bytes(unsigned num_rec, unsigned num_in, size
  * CTA per SM issuing MMAs on shared-memory operands (about 0.1 s): the
  * roofline denominator of that method.  No counterpart in the reference. */
 int par2cuda_tensor_fp4_rate(double* macs_per_s, void* stream);
+/* The number of kernel launches one par2cuda_muladd call with these
+ * arguments makes (the tensor_fp4 method: one per word chunk of expanded
+ * input planes and GEMM, plus the coefficient expansion).  No counterpart in
+ * the reference. */
+int par2cuda_muladd_launches(unsigned num_rec, unsigned num_in, size_t n_words, int method, size_t scratch_bytes);
 /* rec[r][0..n_words) (^)= sum_i coeff[r*num_in + i] * in[i][0..n_words),
  * the run_kernel body (gf16/controller_cpu.cpp:488-515).  Pitches are in
  * 16-bit words (even); rows must be readable/writable up to

@@ -88,6 +88,7 @@ SIGNATURES = [
     ("par2cuda_comb_shape_for", _i, [_u]),
     ("par2cuda_md5_chain_rate", _i, [ctypes.POINTER(ctypes.c_double), _vp]),
     ("par2cuda_muladd_scratch_bytes", _sz, [_u, _u]),
+    ("par2cuda_muladd_launches", _i, [_u, _u, _sz, _i, _sz]),
     ("par2cuda_muladd", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _i, _vp, _sz, _vp]),
     ("par2cuda_muladd_noalloc", _i, [_vp, _sz, _u, _vp, _vp, _sz, _u, _sz, _i, _vp]),
     ("par2cuda_rows_checksum", _i, [_vp, _sz, _u, _vp, _sz, _i, _vp, _vp, _vp]),

@@ -308,9 +308,20 @@ class BatchRunner:
         return all(bool(b.d_flags.all()) for b in self.bufs)
 
     def launches_per_run(self):
+        """Kernel launches of one run_batched() in the current mode."""
         n = 0
         for p in range(self.P):
             live = [b for b in self.bufs if b.window(p)[1] > 0]
             n += len(live) * 5  # synth, cksum partial + finish, verify partial + finish
-            n += len({self.shapes[i] for i, b in enumerate(self.bufs) if b.window(p)[1] > 0})
+            if self.mode == "persistent":
+                n += len({self.shapes[i] for i, b in enumerate(self.bufs) if b.window(p)[1] > 0})
+                continue
+            for b in live:
+                method = self.method_of(b.spec.R)
+                if method == "comb":
+                    n += 1   # the comb kernel from the resident index bytes
+                else:
+                    nw = self._n_words(b.window(p)[1])
+                    sb = autotune.scratch_bytes(method, b.spec.R, b.spec.N, self._n_words(b.W))
+                    n += self.L.par2cuda_muladd_launches(b.spec.R, b.spec.N, nw, autotune.METHODS[method], sb)
         return n

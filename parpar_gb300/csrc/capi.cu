@@ -174,6 +174,17 @@ size_t par2cuda_tensor_fp4_scratch_bytes(unsigned num_rec, unsigned num_in, size
 	return p2c::tc4_scratch_bytes(num_rec, num_in, n_words);
 }
 
+int par2cuda_muladd_launches(unsigned num_rec, unsigned num_in, size_t n_words, int method, size_t scratch_bytes) {
+	if(!num_rec || !n_words) return 0;
+	switch(method) {
+	case PAR2CUDA_METHOD_XOR: case PAR2CUDA_METHOD_NIBBLE: return 1;
+	case PAR2CUDA_METHOD_TENSOR: return 2;
+	case PAR2CUDA_METHOD_TENSOR_FP4: return (int)p2c::tc4_launches(num_rec, num_in, n_words, scratch_bytes);
+	case PAR2CUDA_METHOD_AUTO: case PAR2CUDA_METHOD_COMB: return 2;
+	default: p2c::set_error("unknown method %d", method); return -1;
+	}
+}
+
 int par2cuda_muladd(const uint16_t* d_in, size_t in_pitch_words, unsigned num_in, const uint16_t* d_coeff,
                     uint16_t* d_rec, size_t rec_pitch_words, unsigned num_rec, size_t n_words, int accumulate,
                     int method, void* d_scratch, size_t scratch_bytes, void* stream) {

@@ -491,6 +491,15 @@ size_t tc4_scratch_chunked_bytes(unsigned R, unsigned nIn, size_t nWords, size_t
 	return std::min(tc4_scratch_bytes(R, nIn, nWords), T4_HDR_BYTES + t4_bbytes(R, nIn) + round_up(aMin, 1024));
 }
 
+unsigned tc4_launches(unsigned R, unsigned nIn, size_t nWords, size_t scratchBytes) {
+	if(!R || !nWords || !nIn) return 0;
+	const size_t kBytes = t4_kbytes(nIn), bBytes = t4_bbytes(R, nIn);
+	if(scratchBytes < T4_HDR_BYTES + bBytes + (size_t)T4_BM * kBytes) return 0;
+	size_t wChunk = (scratchBytes - T4_HDR_BYTES - bBytes) / kBytes / T4_BM * T4_BM;
+	wChunk = std::min(wChunk, round_up(nWords, T4_BM));
+	return 1 + 2 * (unsigned)((nWords + wChunk - 1) / wChunk);   // coefficients, then per chunk: inputs + GEMM
+}
+
 int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t* coeff, uint16_t* rec, size_t recPitch,
                unsigned R, size_t nWords, int accumulate, void* scratch, size_t scratchBytes, cudaStream_t st)
 {

@@ -110,7 +110,9 @@ class ResidentJob:
         # soon as an SM frees, ahead of pending multiply-accumulate CTAs of
         # other jobs in flight
         self.sb = stream_b or torch.cuda.Stream(device=dev, priority=-10)
-        self.launches_per_run = 8
+        # checksum (2), the multiply-accumulate, verification (2), IFSC, file MD5
+        self.launches_per_run = 6 + self.L.par2cuda_muladd_launches(self.R, self.N, self.row_words, method,
+                                                                    self.scratch_bytes)
 
     def set_input_nums(self, input_nums):
         """PAR2 input number of every row (e.g. once the file order by file ID

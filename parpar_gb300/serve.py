@@ -170,7 +170,12 @@ class Server:
                 torch.minimum(d_ok, d_flags.min().reshape(1), out=d_ok)
                 if self.digests:
                     host_out.append(d_rec.view(torch.uint8)[:, :n].to("cpu", non_blocking=True))
-            self.launches += 7
+            # synth, checksum (2), the multiply-accumulate, verification (2)
+            if self.persistent or method == "comb":
+                self.launches += 6
+            else:
+                self.launches += 5 + L.par2cuda_muladd_launches(spec.R, spec.N, nw, autotune.METHODS[method],
+                                                                 d_scr.numel())
         ev = torch.cuda.Event()
         ev.record(st_obj)
         req.state = dict(tensors=(d_in, d_rec, d_nums, d_exps, d_idx, d_ck, d_flags, counter, descs, d_coeff, d_scr),

@@ -88,6 +88,7 @@ class JobStream:
         if method == _lib.METHOD_TENSOR_FP4:
             self.scratch_bytes = L.par2cuda_tensor_fp4_scratch_bytes(R, N, self.row_words)
         self.d_scratch = torch.empty(max(self.scratch_bytes, 256), dtype=torch.uint8, device=dev)
+        self.muladd_launches = L.par2cuda_muladd_launches(R, N, self.row_words, method, self.scratch_bytes)
         self.d_ck = torch.empty(max(N, R) * 8, dtype=torch.uint8, device=dev)
         # file MD5 tables of one group: the files of its `group` slots in
         # slot order, rows counted from the group's first row
@@ -344,7 +345,9 @@ class JobStream:
         _lib.check(L.par2cuda_slice_hash(d_in, self.pitch, N, self.d_lens.data_ptr(), self.S,
                                         self.d_ifsc[s].data_ptr(), side.cuda_stream), "slice_hash")
         self.ev_ifsc[s] = self._event(side, timing)
-        self.launches += 7   # checksum (2 kernels), coefficient index, contraction, verification (2), IFSC
+        # checksum (2 kernels), the multiply-accumulate's own launches,
+        # verification (2), IFSC
+        self.launches += 5 + self.muladd_launches
         rec["gf"], rec["ifsc"] = self.ev_gf[s], self.ev_ifsc[s]
         self.jobs_done.append(rec)
 

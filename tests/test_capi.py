@@ -43,6 +43,24 @@ def test_host_helpers_without_gpu():
     assert lib.par2cuda_muladd_scratch_bytes(10, 100) == (max(10 * 13 * 16, 10 * 100 * 32) + 255) // 256 * 256
 
 
+def test_launch_counts_without_gpu():
+    lib = _lib.load()
+    assert lib.par2cuda_muladd_launches(200, 2000, 1 << 20, _lib.METHOD_COMB, 0) == 2
+    assert lib.par2cuda_muladd_launches(200, 2000, 1 << 20, _lib.METHOD_XOR, 0) == 1
+    assert lib.par2cuda_muladd_launches(0, 2000, 1 << 20, _lib.METHOD_COMB, 0) == 0
+    # tensor_fp4: coefficient expansion, then per word chunk the input planes
+    # and the GEMM; a chunk holds what the scratch leaves after the fixed part
+    R, N, nw = 200, 2000, 1048580
+    kbytes = (N + 15) // 16 * 16 * 8
+    one_tile = (128 * kbytes + 1023) // 1024 * 1024
+    fixed = lib.par2cuda_tensor_fp4_scratch_bytes(R, N, 1) - one_tile
+    full = lib.par2cuda_tensor_fp4_scratch_bytes(R, N, nw)
+    chunk_words = (full - fixed) // kbytes // 128 * 128
+    assert lib.par2cuda_muladd_launches(R, N, nw, _lib.METHOD_TENSOR_FP4, full) == 1 + 2 * -(-nw // chunk_words)
+    assert lib.par2cuda_muladd_launches(R, N, nw, _lib.METHOD_TENSOR_FP4, fixed + 128 * kbytes) == 1 + 2 * -(-nw // 128)
+    assert lib.par2cuda_muladd_launches(R, N, nw, _lib.METHOD_TENSOR_FP4, fixed) == 0   # too small: the call fails
+
+
 def test_create_fails_cleanly_without_device():
     lib = _lib.load()
     h = ctypes.c_void_p()
