@@ -210,9 +210,10 @@ int par2cuda_wait_selftest(unsigned polls, int* gave_up, double* seconds);
 /* Scratch bytes par2cuda_muladd needs for (num_rec, num_in). */
 size_t par2cuda_muladd_scratch_bytes(unsigned num_rec, unsigned num_in);
 /* Scratch bytes par2cuda_muladd needs for method PAR2CUDA_METHOD_TENSOR_FP4:
- * the coefficient bit matrix (16 * roundup(num_rec, 16) rows of
- * roundup(num_in, 16) * 8 bytes) plus the 4-bit input planes of a chunk of at
- * most 1 GiB of words (more scratch = larger chunks; at least one 128-word
+ * a 1 KiB header (the GEMM's tile counter, reset by every call), the
+ * coefficient bit matrix (16 * roundup(num_rec, 48) rows of
+ * roundup(num_in, 16) * 8 bytes) and the 4-bit input planes of a chunk of at
+ * most 1 GiB of words (less scratch = smaller chunks; at least one 128-word
  * tile).  No counterpart in the reference. */
 size_t par2cuda_tensor_fp4_scratch_bytes(unsigned num_rec, unsigned num_in, size_t n_words);
 /* Measures the tensor pipe's rate (binary multiply-accumulates per second)
