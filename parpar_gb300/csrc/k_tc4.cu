@@ -113,6 +113,51 @@ __global__ void __launch_bounds__(256) k_tc4_prep_in(const uint16_t* __restrict_
 	}
 }
 
+// The same with 16-byte loads and stores, for inputs whose base and pitch are
+// 16-byte aligned.  Block: 64 inputs x 128 words; thread t loads 8-word
+// segments (t & 15) of rows t / 16 + 16k, and writes, for the input pair
+// 2 (t & 31), 2 (t & 31) + 1, the 16 bytes of words t / 32 + 8k.  A segment is
+// loaded only when its first word is below nWords (rows are readable up to
+// roundup(nWords, 64) words); words past nWords are zero.
+__global__ void __launch_bounds__(256) k_tc4_prep_in_v(const uint16_t* __restrict__ in, size_t inPitch, unsigned nIn,
+                                                     size_t nWords, size_t w0, uint8_t* __restrict__ A, size_t kBytes)
+{
+	__shared__ uint16_t tile[64][130];
+	const unsigned i0 = blockIdx.y * 64;
+	const size_t wt = w0 + (size_t)blockIdx.x * 128;
+	const unsigned t = threadIdx.x;
+#pragma unroll
+	for(int k = 0; k < 4; k++) {
+		const unsigned ii = (t >> 4) + 16 * k, seg = t & 15;
+		const unsigned i = i0 + ii;
+		const size_t w = wt + 8 * seg;
+		uint4 v = make_uint4(0, 0, 0, 0);
+		if(i < nIn && w < nWords) {
+			v = __ldg(reinterpret_cast<const uint4*>(in + (size_t)i * inPitch + w));
+			const size_t valid = nWords - w;
+			if(valid < 8) {
+				uint32_t* e = reinterpret_cast<uint32_t*>(&v);
+#pragma unroll
+				for(int q = 0; q < 4; q++) {
+					if((size_t)(2 * q) >= valid) e[q] = 0;
+					else if((size_t)(2 * q + 1) >= valid) e[q] &= 0xFFFFu;
+				}
+			}
+		}
+		uint32_t* row = reinterpret_cast<uint32_t*>(&tile[ii][8 * seg]);
+		row[0] = v.x; row[1] = v.y; row[2] = v.z; row[3] = v.w;
+	}
+	__syncthreads();
+	const unsigned ip = t & 31;
+	if((size_t)(i0 + 2 * ip) * 8 >= kBytes) return;
+#pragma unroll 4
+	for(unsigned ww = t >> 5; ww < 128; ww += 8) {
+		const uint2 a = t4_spread16(tile[2 * ip][ww]), b = t4_spread16(tile[2 * ip + 1][ww]);
+		*reinterpret_cast<uint4*>(A + ((size_t)blockIdx.x * 128 + ww) * kBytes + (size_t)(i0 + 2 * ip) * 8) =
+			make_uint4(a.x, a.y, b.x, b.y);
+	}
+}
+
 // B: rows 16r + j for r < rPad (zero rows past R), 8 bytes per input; one
 // thread per (r, i).
 __global__ void __launch_bounds__(256) k_tc4_prep_coeff(const uint16_t* __restrict__ coeff, unsigned R, unsigned nIn,
@@ -554,8 +599,13 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 	unsigned base = 0;
 	for(size_t w0 = 0; w0 < nWords; w0 += wChunk) {
 		const size_t rows = std::min(wChunk, round_up(nWords - w0, T4_BM));
-		dim3 pg((unsigned)(rows / 64), (nInPad + 63) / 64);
-		k_tc4_prep_in<<<pg, 256, 0, st>>>(in, inPitch, nIn, nWords, w0, A, kBytes);
+		if((reinterpret_cast<uintptr_t>(in) & 15) == 0 && (inPitch & 7) == 0) {
+			dim3 pg((unsigned)(rows / 128), (nInPad + 63) / 64);
+			k_tc4_prep_in_v<<<pg, 256, 0, st>>>(in, inPitch, nIn, nWords, w0, A, kBytes);
+		} else {
+			dim3 pg((unsigned)(rows / 64), (nInPad + 63) / 64);
+			k_tc4_prep_in<<<pg, 256, 0, st>>>(in, inPitch, nIn, nWords, w0, A, kBytes);
+		}
 		P2C_CUDA_TRY(cudaGetLastError());
 		CUtensorMap tmA;
 		if(t4_map(&tmA, A, kBytes, rows, T4_BM)) return -1;

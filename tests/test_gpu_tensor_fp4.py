@@ -11,12 +11,14 @@ from parpar_gb300 import _lib, synth
 pytestmark = pytest.mark.gpu
 
 
-def run_fp4(n, R, S, seed, accumulate=False, scratch_bytes=None, shape=0):
+def run_fp4(n, R, S, seed, accumulate=False, scratch_bytes=None, shape=0, pitch_pad=0):
     import torch
     L = _lib.load()
     prev = L.par2cuda_set_tc4_shape(shape)
     pitch = L.par2cuda_row_pitch_bytes(S)
-    pw = pitch // 2
+    # pitch_pad words more per row: a pitch that is not a multiple of 16 bytes
+    # takes the input expansion's 2-byte-load path
+    pw = pitch // 2 + pitch_pad
     x = synth.slices(seed, 0, n, S)
     d_in = torch.zeros((n, pw), dtype=torch.int16, device="cuda")
     d_in.view(torch.uint8)[:, :S].copy_(torch.from_numpy(x))
@@ -52,9 +54,16 @@ def run_fp4(n, R, S, seed, accumulate=False, scratch_bytes=None, shape=0):
     (200, 33, 65536),     # several K blocks, three recovery tiles
     (40, 100, 131072),    # 7 or 9 recovery tiles x 512 word tiles: accumulators reused, many tiles per CTA
     (1100, 30, 20000),    # 69 k-blocks (the automatic choice takes the 16-slice tile)
+    (37, 20, 4100),       # 2050 words: the last 8-word load segment is partly past the words
 ])
 def test_fp4_matches_oracle(n, R, S, shape):
     got, want = run_fp4(n, R, S, seed=n * 31 + R, shape=shape)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("n,R,S", [(37, 20, 4100), (70, 33, 10002)])
+def test_fp4_unaligned_pitch(n, R, S):
+    got, want = run_fp4(n, R, S, seed=n + R, pitch_pad=2)
     assert np.array_equal(got, want)
 
 
