@@ -52,6 +52,13 @@ UNIT = "mul-adds/s"
 # dram__bytes_read.sum + dram__bytes_write.sum, and the algorithmic (N + R) x S
 # one ncu capture of k_file_md5 (4 files, 266.6 MB in all): DRAM bytes per byte hashed
 MD5_TRAFFIC = (272723456 + 4043776, 266590293)
+# k_tc4_gemm, one launch (one word chunk) captured by ncu: DRAM read + write,
+# the chunk's expanded input-plane bytes; keyed by (inputs, recovery)
+TC4_TRAFFIC = {
+    (2000, 200): (3963986944 + 29081600, 67072 * 16000,
+                  "k_tc4_gemm on 2000x200x512KiB (first 1 GiB word chunk: the bandwidth workload's chunk shape)"),
+    (4096, 4096): (71958856192 + 272894976, 32768 * 32768, "k_tc4_gemm on the dense workload (first 1 GiB word chunk)"),
+}
 KERNEL_TRAFFIC = {
     "k_comb_pair": (270406912 + 87077120, (512 + 200) * 524288, "k_comb_pair<6,12,2> on 512x200x512KiB"),
     "k_comb_pair_rr": (268913408 + 81736448, (512 + 192) * 524288, "k_comb_pair_rr<8,12,2,152,56> on 512x192x512KiB"),
@@ -70,6 +77,10 @@ WORKLOADS = {
                     desc="512 input slices x 512 KiB, 192 recovery, GF contraction only (ncu capture size)"),
     "profile_ws": dict(S=524288, N=512, files=1, R=200, hashes=False,
                        desc="512 input slices x 512 KiB, 200 recovery, GF contraction only (ncu capture size, 72-row CTAs)"),
+    "profile_bw": dict(S=524288, N=2000, files=1, R=200, hashes=False,
+                       desc="2000 input slices x 512 KiB, 200 recovery, GF contraction only (ncu capture size: the "
+                            "bandwidth workload's inputs and recovery count, so each 1 GiB word chunk of the 4-bit "
+                            "tensor method has the full-size launch's shape)"),
     "profile_hash": dict(S=1048576, N=256, files=4, R=8, hashes=True,
                          desc="256 input slices x 1 MiB over 4 files, 8 recovery, with hashing (ncu capture size)"),
     # the bandwidth workload as files on the host's disk: files in, finished .par2 files out
@@ -678,14 +689,34 @@ def roofline_gf(mul_adds, muladd_ms, lop3_ops, n_sm, sm_mhz, kname, alg_bytes):
     return out
 
 
-def roofline_tensor(mul_adds, muladd_ms, mma_macs, kname):
+def tc4_gemm_traffic(N, R, n_words):
+    """DRAM bytes of the GEMM launches of one tensor_fp4 call: the ncu capture
+    of one launch of the same (inputs, recovery) shape, scaled by the call's
+    expanded input-plane bytes (every launch but the last takes a 1 GiB word
+    chunk); None for shapes without a capture."""
+    cap = TC4_TRAFFIC.get((N, R))
+    if cap is None:
+        return None
+    a_call = (N + 15) // 16 * 16 * 8 * ((n_words + 127) // 128 * 128)
+    return cap[0] / cap[1] * a_call
+
+
+def tc4_traffic_source(N, R):
+    cap = TC4_TRAFFIC.get((N, R))
+    return None if cap is None else ("ncu dram__bytes_read+write of %s: %.2f GB for %.2f GB of expanded input "
+                                     "planes, scaled by this call's expanded input bytes" %
+                                     (cap[2], cap[0] / 1e9, cap[1] / 1e9))
+
+
+def roofline_tensor(mul_adds, muladd_ms, mma_macs, kname, traffic=None, traffic_source=None):
     """Tensor roofline of the block-scaled 4-bit form: 256 binary
     multiply-accumulates (512 flops) per word mul-add against the MMA rate of
     the same instruction measured on this device (par2cuda_tensor_fp4_rate);
     the call's time includes its two operand-preparation kernels."""
     flops = mul_adds * 512 / (muladd_ms / 1e3)
     return {"bound": "tensor", "kernel": kname, "achieved": flops / 1e12, "peak": 2 * mma_macs / 1e12,
-            "unit": "TFLOP/s", "frac": flops / (2 * mma_macs), "traffic": None,
+            "unit": "TFLOP/s", "frac": flops / (2 * mma_macs), "traffic": traffic,
+            "traffic_source": traffic_source if traffic else None,
             "peak_source": "measured: k_tc4_mma_rate, tcgen05.mma kind::mxf4 M=128 N=256 K=64 back to back on "
                            "shared-memory operands, one CTA per SM (nominal dense fp4 of the part: 13.5 PFLOP/s)",
             "mul_adds_per_s": mul_adds / (muladd_ms / 1e3), "muladd_ms": muladd_ms}
@@ -792,7 +823,8 @@ def run_ours(args, cfg, file_lens):
     rgf = roofline_gf(mul_adds, muladd_ms, lop3.value, n_sm, sm_mhz, kname, alg_bytes)
     if args.traffic_bytes:
         rgf["traffic"] = args.traffic_bytes
-    rtc = roofline_tensor(mul_adds, muladd_ms, fp4_rate.value, kname) if args.method == "tensor_fp4" else None
+    rtc = roofline_tensor(mul_adds, muladd_ms, fp4_rate.value, kname, tc4_gemm_traffic(N, R, ((S + 7) // 8 * 8 + 8) // 2),
+                          tc4_traffic_source(N, R)) if args.method == "tensor_fp4" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -853,7 +885,9 @@ def run_ours(args, cfg, file_lens):
                          "roofline_gf": roofline_gf(d_mul, dense["muladd_ms"], lop3.value, n_sm, sm_mhz, dk,
                                                     (dm["N"] + dm["R"]) * dm["S"])}
         if args.dense_method == "tensor_fp4":
-            line["dense"]["roofline_tensor"] = roofline_tensor(d_mul, dense["muladd_ms"], fp4_rate.value, dk)
+            line["dense"]["roofline_tensor"] = roofline_tensor(
+                d_mul, dense["muladd_ms"], fp4_rate.value, dk,
+                tc4_gemm_traffic(dm["N"], dm["R"], ((dm["S"] + 7) // 8 * 8 + 8) // 2), tc4_traffic_source(dm["N"], dm["R"]))
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_run(cfg, file_lens, os.cpu_count() or 1)
     print(json.dumps(line))

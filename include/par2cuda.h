@@ -180,6 +180,12 @@ int par2cuda_set_comb_shape(int shape);
  * next tile's MMAs).  Returns the previous setting.  No counterpart in the
  * reference. */
 int par2cuda_set_tc4_shape(int shape);
+/* Raster group of the tensor_fp4 GEMM for every later call in this process
+ * (the autotuner's knob): the number of 128-word tiles that walk the recovery
+ * tiles together; 0 = chosen from the input count (as many as keep their
+ * expanded input planes in about 48 MiB of L2).  Returns the previous
+ * setting.  No counterpart in the reference. */
+int par2cuda_set_tc4_group(int word_tiles);
 /* The tile shape (1 or 2) the next tensor_fp4 call with num_in inputs will use. */
 int par2cuda_tc4_shape_for(unsigned num_in);
 /* Measures the rate (bytes/s) of one MD5 stream on one GPU thread with its

@@ -82,6 +82,7 @@ SIGNATURES = [
     ("par2cuda_coeff", _u16, [_u16, _u16]),
     ("par2cuda_set_comb_shape", _i, [_i]),
     ("par2cuda_set_tc4_shape", _i, [_i]),
+    ("par2cuda_set_tc4_group", _i, [_i]),
     ("par2cuda_tc4_shape_for", _i, [_u]),
     ("par2cuda_device_error", _i, []),
     ("par2cuda_lop3_rate", _i, [ctypes.POINTER(ctypes.c_double), _vp]),

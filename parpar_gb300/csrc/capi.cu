@@ -135,6 +135,11 @@ int par2cuda_set_tc4_shape(int shape) {
 	return p2c::set_tc4_shape(shape);
 }
 
+int par2cuda_set_tc4_group(int word_tiles) {
+	if(word_tiles < 0 || word_tiles > 4096) { p2c::set_error("tensor_fp4 raster group %d out of range 0..4096", word_tiles); return -1; }
+	return p2c::set_tc4_group(word_tiles);
+}
+
 int par2cuda_tc4_shape_for(unsigned num_in) { return p2c::tc4_shape_for((unsigned)((num_in + 15) / 16)); }
 
 int par2cuda_md5_chain_rate(double* bytes_per_s, void* stream) {

@@ -508,6 +508,8 @@ static unsigned t4_rpad(unsigned R) { return (unsigned)round_up(R ? R : 1, T4_RC
 
 static std::atomic<int> g_tc4_shape{0};
 int set_tc4_shape(int shape) { return g_tc4_shape.exchange(shape); }
+static std::atomic<int> g_tc4_group{0};
+int set_tc4_group(int groupM) { return g_tc4_group.exchange(groupM); }
 
 // Tile shape for kBlocks k-blocks (16 inputs each) per tile.  The 192-row
 // tile with two accumulators hides each tile's read-out behind the next
@@ -592,7 +594,8 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 	// word tiles per raster group: their A tiles (128 x kBytes each) stay in
 	// L2 (about 48 MiB of it) while the group walks the recovery tiles, so A
 	// is read from HBM once and each B tile once per group
-	const unsigned groupM = (unsigned)std::min<size_t>(64, std::max<size_t>(8, (48ull << 20) / ((size_t)T4_BM * kBytes)));
+	unsigned groupM = (unsigned)std::min<size_t>(64, std::max<size_t>(8, (48ull << 20) / ((size_t)T4_BM * kBytes)));
+	if(g_tc4_group.load() > 0) groupM = (unsigned)g_tc4_group.load();
 	// the tile counter starts at 0 for this call; each launch advances it by
 	// its tiles + CTAs (every CTA's last fetch finds no tile)
 	P2C_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));

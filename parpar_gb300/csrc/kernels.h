@@ -102,6 +102,7 @@ int tc4_muladd(const uint16_t* in, size_t inPitch, unsigned nIn, const uint16_t*
 int tc4_error_take();
 int tc4_mma_rate(double* macsPerSec, cudaStream_t st);
 int set_tc4_shape(int shape);
+int set_tc4_group(int groupM);
 unsigned tc4_launches(unsigned R, unsigned nIn, size_t nWords, size_t scratchBytes);
 int tc4_shape_for(unsigned kBlocks);
 } // namespace p2c
