@@ -1127,8 +1127,10 @@ def run_batched_workload(args, cfg):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    # a step is one whole job; the job stream's timed region cannot be shorter
+    # than one job's longest file MD5 chain (~1.3 s), so K = 20 jobs by default
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="bandwidth")
     ap.add_argument("--no-e2e", action="store_true")
